@@ -1,0 +1,182 @@
+/*
+ * woxel_gb300.h — C ABI of the GB300 (sm_103a) primary-ray pass for woxel's
+ * VDB345 grids: an HDDA march with grid-SDF empty-space skipping.
+ *
+ * The entry points replace woxel's wgpu compute pass (`cp_main`,
+ * src/shaders/raycast.comp.wgsl:60-68, dispatched at
+ * src/render/wgpu_context.rs:270-282) and the grid upload that feeds it
+ * (src/render/wgpu_context.rs:101-159). Inputs keep the reference's own data:
+ * the 256-byte ComputeState uniform (src/render/gpu_types/compute_state.rs:9-29)
+ * and the flattened VDB345 view (masks()/origins()/atlas(),
+ * src/vdb/vdb345.rs:108-264). Outputs are RGBA8 (the rgba8unorm storage texture
+ * of src/render/gpu_types/texture.rs:25-75) plus an optional per-pixel hit record.
+ *
+ * Conventions: every function returns an int status (WX_OK == 0); nothing
+ * aborts or throws across this boundary. A context is used from one host
+ * thread at a time; grids are immutable after upload and may be used from any
+ * stream of the context's device. Pointers named *_dev are device pointers;
+ * output pointers of wx_render may be device or host memory (host memory is
+ * staged through the context and copied back on the given stream).
+ */
+#ifndef WOXEL_GB300_H
+#define WOXEL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define WX_OK 0
+#define WX_ERR_INVALID 1      /* bad argument or malformed grid */
+#define WX_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define WX_ERR_OOM 3          /* device or host allocation failed */
+#define WX_ERR_UNSUPPORTED 4  /* valid input outside what this build handles */
+#define WX_ERR_BUDGET 5       /* request does not fit the memory budget */
+#define WX_ERR_TIMEOUT 6      /* a bounded wait expired */
+#define WX_ERR_CANCELLED 7    /* work was cancelled */
+
+/* ---- render modes (src/render/egui_dev.rs:11-18) ---- */
+#define WX_MODE_GRAY 0u
+#define WX_MODE_RGB 1u
+#define WX_MODE_RAY 2u
+#define WX_MODE_DIFFUSE 3u
+#define WX_MODE_GLOSSY 4u
+
+/* 256-byte uniform; field order and padding of ComputeState
+ * (src/render/gpu_types/compute_state.rs:9-29). Matrices are column-major. */
+typedef struct wx_state_uniform {
+    float view_projection[16];
+    float camera_to_world[16];
+    float eye[4];
+    float u[4];
+    float mv[4];
+    float wp[4];
+    uint32_t render_mode[4];
+    uint32_t show_345[4];
+    float sun_dir[4];
+    float sun_color[4]; /* alpha = intensity */
+} wx_state_uniform;
+
+/* Per-pixel result of the primary ray (no counterpart in the reference,
+ * which only writes colour). 32 bytes. */
+typedef struct wx_hit {
+    float p[3];        /* march position when hdda_ray returned; floor(p) is the voxel ijk */
+    float t;           /* dot(p - eye, dir) = ((dx*dir.x + dy*dir.y) + dz*dir.z), FP32 */
+    uint32_t node;     /* DFS pool index of the deepest cached node (the leaf when
+                          level == 3); 0xFFFFFFFF when level == 0 */
+    uint32_t info;     /* bits 0-1 state (0 hit, 1 out of bounds, 2 step cap),
+                          bits 2-3 level (cached parents, 0..3), bits 4-6 last step
+                          mask x,y,z, bits 8-18 loop iteration i */
+    uint32_t shadow;   /* mode 3: bit 0 shadow ray traced, bits 1-2 its state,
+                          bits 8-18 its iteration count; 0 otherwise */
+    uint32_t reserved;
+} wx_hit;
+
+/* The flattened grid exactly as woxel's Rust side holds it:
+ *   masks()   src/vdb/vdb345.rs:119-161 (u64 words split lo/hi, DFS order)
+ *   origins() src/vdb/vdb345.rs:108-117 (sorted root keys; x,y,z + stride pad)
+ *   atlas()   src/vdb/vdb345.rs:163-264 as uploaded by src/render/wgpu_context.rs:119-151:
+ *             an R32Uint 3-D texture whose texel (x,y,z) sits at (z*H + y)*W + x. */
+typedef struct wx_vdb345_view {
+    const uint32_t *kids5, *vals5; /* n5 * 1024 words each */
+    const uint32_t *kids4, *vals4; /* n4 * 128 words each */
+    const uint32_t *vals3;         /* n3 * 16 words */
+    const int32_t *origins;        /* n5 entries of origin_stride int32 (x, y, z, ...) */
+    uint64_t n5, n4, n3;
+    uint32_t origin_stride;        /* 3 or 4 (the reference's storage buffer uses 4) */
+    const uint32_t *atlas[3];      /* N5, N4, N3 atlases */
+    uint32_t dims[3][3];           /* W, H, D of each atlas */
+} wx_vdb345_view;
+
+typedef struct wx_grid_info {
+    uint64_t n5, n4, n3;           /* node counts per level */
+    uint64_t device_bytes;         /* bytes of device node pools */
+    uint64_t active_voxels;        /* popcount of the leaf value masks */
+} wx_grid_info;
+
+typedef struct wx_ctx wx_ctx;
+typedef struct wx_grid wx_grid;
+typedef struct wx_topology wx_topology;
+
+/* ---- library ---- */
+const char *wx_status_string(int status);
+/* Last error message of the calling thread (for calls without a context). */
+const char *wx_thread_last_error(void);
+const char *wx_version(void);
+
+/* ---- context: replaces WgpuContext's device/queue (wgpu_context.rs:38-99) ---- */
+int wx_ctx_create(int device, wx_ctx **out);
+int wx_ctx_destroy(wx_ctx *ctx);
+const char *wx_last_error(const wx_ctx *ctx);
+
+/* ---- grids: replace the atlas/mask upload (wgpu_context.rs:101-159, 506-573) ---- */
+/* Drop-in: repack the Rust side's flattened view into device node pools. */
+int wx_grid_upload(wx_ctx *ctx, const wx_vdb345_view *view, wx_grid **out);
+/* Native: compute the per-level SDF (vdb345.rs:290-670) on the host and pack
+ * the pools directly from a topology, without the padded atlas. */
+int wx_grid_build(wx_ctx *ctx, wx_topology *topo, wx_grid **out);
+int wx_grid_release(wx_ctx *ctx, wx_grid *grid);
+int wx_grid_get_info(const wx_grid *grid, wx_grid_info *out);
+
+/* ---- the raycast pass: replaces cp_main (raycast.comp.wgsl:60-68) ---- */
+/* Renders the (8*floor(w/8)) x (4*floor(h/4)) pixels the reference dispatch
+ * covers (wgpu_context.rs:281); other pixels are not written. rgba8 holds
+ * w*h*4 bytes row-major; hits (w*h records) may be NULL. stream is a
+ * cudaStream_t (NULL = legacy default stream). */
+int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, uint32_t width,
+              uint32_t height, uint8_t *rgba8, wx_hit *hits, void *stream);
+
+/* ---- host-side helpers (no GPU needed) ---- */
+/* ComputeState::build (compute_state.rs:87-131) for a look_at_rh camera
+ * (camera.rs:31-35). show_345 may be NULL. */
+int wx_state_build(const float eye[3], const float target[3], const float up[3], float aspect,
+                   float fovy_deg, float resolution_width, uint32_t render_mode,
+                   const uint32_t show_345[3], const float sun_dir[3], const float sun_color[3],
+                   float sun_intensity, wx_state_uniform *out);
+/* SunSettings::default (egui_dev.rs:355-368). */
+void wx_sun_default(float dir[3], float color[3], float *intensity);
+
+/* Topology: the node structure of a VDB345 grid (child/value masks, DFS order). */
+int wx_topology_from_masks(const uint32_t *kids5, const uint32_t *vals5, uint64_t n5,
+                           const uint32_t *kids4, const uint32_t *vals4, uint64_t n4,
+                           const uint32_t *vals3, uint64_t n3, const int32_t *origins,
+                           uint32_t origin_stride, wx_topology **out);
+/* As set_voxel (vdb345.rs:26-66) on each ijk. */
+int wx_topology_from_voxels(const int32_t *ijk, uint64_t n, wx_topology **out);
+/* Leaves given as 8-aligned origins (x,y,z) and 8 u64 value-mask words each. */
+int wx_topology_from_leaves(const int32_t *origins, const uint64_t *masks, uint64_t n,
+                            wx_topology **out);
+void wx_topology_free(wx_topology *topo);
+int wx_topology_counts(const wx_topology *topo, uint64_t counts[3]);
+uint64_t wx_topology_active_voxels(const wx_topology *topo);
+/* masks()/origins() export; origins written with stride 4 (x,y,z,0). */
+int wx_topology_masks(const wx_topology *topo, uint32_t *kids5, uint32_t *vals5,
+                      uint32_t *kids4, uint32_t *vals4, uint32_t *vals3, int32_t *origins);
+/* compute_sdf (vdb345.rs:290-670); nthreads <= 0 picks the hardware count. */
+int wx_topology_sdf(wx_topology *topo, int nthreads);
+/* atlas() export in the uploaded texture layout; side[3] = 32*d5, 16*d4, 8*d3.
+ * Pass NULL atlases to query sides. Leaf value texels are written as value_texel. */
+int wx_topology_atlas(const wx_topology *topo, uint32_t side[3], uint32_t *a5, uint32_t *a4,
+                      uint32_t *a3, uint32_t value_texel);
+
+/* ---- synthetic grids (seeded; f32 narrow-band level sets use value = signed distance) ---- */
+/* Voxels with |(|ijk - c| - r)| < band are active. */
+int wx_gen_sphere(float cx, float cy, float cz, float radius, float band, wx_topology **out);
+/* Union of `count` spheres, radii U[rmin, rmax], centres U[lo, hi)^3. */
+int wx_gen_spheres(uint32_t count, float rmin, float rmax, float lo, float hi, float band,
+                   uint64_t seed, wx_topology **out);
+/* Leaves on the 8^3 lattice of [lo, lo + extent)^3 kept where 3-octave value
+ * noise exceeds the quantile giving `occupancy`; voxels active with p_voxel. */
+int wx_gen_noise_leaves(int32_t lo, uint32_t extent, double occupancy, double p_voxel,
+                        uint64_t seed, int nthreads, wx_topology **out);
+/* Orbit eyes at `radius` around the origin, directions uniform on the sphere
+ * with |y| <= 0.9 * radius (keeps look_at_rh's +y up well conditioned). */
+int wx_orbit_eyes(uint32_t count, float radius, uint64_t seed, float *eyes_xyz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,209 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
+CPU-baseline / reference arms of bench.py as the checker. The product never
+imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "liboracle.so"
+
+HIT_DTYPE = np.dtype([("p", "<f4", (3,)), ("t", "<f4"), ("node", "<u4"), ("info", "<u4"),
+                      ("shadow", "<u4"), ("reserved", "<u4")])
+STATS_DTYPE = np.dtype([("steps", "<u4"), ("bytes", "<u4"), ("shadow_steps", "<u4"), ("shadow_bytes", "<u4"),
+                        ("grazing", "<u4"), ("reserved", "<u4", (3,))])
+
+
+class orc_view(C.Structure):
+    _fields_ = [("kids5", C.c_void_p), ("vals5", C.c_void_p), ("kids4", C.c_void_p), ("vals4", C.c_void_p),
+                ("vals3", C.c_void_p), ("origins", C.c_void_p), ("n5", C.c_uint64), ("n4", C.c_uint64),
+                ("n3", C.c_uint64), ("atlas", C.c_void_p * 3), ("dims", (C.c_uint32 * 3) * 3)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+        L = C.CDLL(str(LIB_PATH))
+        P, U64, I = C.c_void_p, C.c_uint64, C.c_int
+        sig = {
+            "orc_global_to_node": (None, [P, I, P]),
+            "orc_global_to_offset": (U64, [P, I, I]),
+            "orc_offset_to_child": (None, [U64, I, P]),
+            "orc_child_to_offset": (U64, [P, I]),
+            "orc_tree_new": (P, []),
+            "orc_tree_free": (None, [P]),
+            "orc_set_voxel": (None, [P, P, C.c_uint32]),
+            "orc_get_voxel": (I, [P, P, P, P]),
+            "orc_tree_from_masks": (P, [P, P, U64, P, P, U64, P, U64, P]),
+            "orc_count_nodes": (None, [P, P]),
+            "orc_compute_sdf": (None, [P]),
+            "orc_masks": (None, [P, P, P, P, P, P, P]),
+            "orc_atlas": (None, [P, P, P, P, P]),
+            "orc_state_build": (None, [P, P, P, C.c_float, C.c_float, C.c_float, C.c_uint32, P, P, P,
+                                       C.c_float, P]),
+            "orc_render": (I, [P, P, C.c_uint32, C.c_uint32, P, P, P, I]),
+            "orc_render_tiles": (I, [P, P, C.c_uint32, C.c_uint32, U64, U64, P, P, P, I]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+# ---- coordinate maths (data_structure.rs:43-91) ----
+def global_to_node(g, total_log2: int):
+    a = np.asarray(g, np.int32)
+    out = np.zeros(3, np.int32)
+    lib().orc_global_to_node(a.ctypes.data, total_log2, out.ctypes.data)
+    return tuple(int(x) for x in out)
+
+
+def global_to_offset(g, log2d: int, total_log2: int) -> int:
+    a = np.asarray(g, np.int32)
+    return int(lib().orc_global_to_offset(a.ctypes.data, log2d, total_log2))
+
+
+def offset_to_child(off: int, log2d: int):
+    out = np.zeros(3, np.uint32)
+    lib().orc_offset_to_child(off, log2d, out.ctypes.data)
+    return tuple(int(x) for x in out)
+
+
+def child_to_offset(c, log2d: int) -> int:
+    a = np.asarray(c, np.uint32)
+    return int(lib().orc_child_to_offset(a.ctypes.data, log2d))
+
+
+class Tree:
+    """The reference VDB345 tree restated in C (vdb345.rs)."""
+
+    def __init__(self, handle=None):
+        self._h = C.c_void_p(handle if handle is not None else lib().orc_tree_new())
+
+    def __del__(self):
+        try:
+            if self._h and self._h.value:
+                lib().orc_tree_free(self._h)
+        except Exception:
+            pass
+
+    @classmethod
+    def from_voxels(cls, ijk, values=None) -> "Tree":
+        t = cls()
+        a = np.ascontiguousarray(ijk, np.int32).reshape(-1, 3)
+        vals = np.ones(a.shape[0], np.uint32) if values is None else np.asarray(values, np.uint32)
+        for i in range(a.shape[0]):
+            t.set_voxel(a[i], int(vals[i]))
+        return t
+
+    @classmethod
+    def from_masks(cls, m: dict) -> "Tree":
+        k5, v5, k4, v4, v3 = (np.ascontiguousarray(m[k], np.uint32) for k in ("kids5", "vals5", "kids4", "vals4", "vals3"))
+        org = np.ascontiguousarray(m["origins"], np.int32).reshape(-1, 4)
+        h = lib().orc_tree_from_masks(k5.ctypes.data, v5.ctypes.data, k5.size // 1024, k4.ctypes.data,
+                                      v4.ctypes.data, k4.size // 128, v3.ctypes.data, v3.size // 16, org.ctypes.data)
+        if not h:
+            raise ValueError("masks do not describe a consistent tree")
+        return cls(h)
+
+    def set_voxel(self, p, value: int = 1) -> None:
+        a = np.asarray(p, np.int32)
+        lib().orc_set_voxel(self._h, a.ctypes.data, value)
+
+    def get_voxel(self, p):
+        a = np.asarray(p, np.int32)
+        v, lvl = C.c_uint64(), C.c_int()
+        kind = lib().orc_get_voxel(self._h, a.ctypes.data, C.byref(v), C.byref(lvl))
+        return ["Offs", "Leaf", "Innr", "Root", "Bkgr"][kind], int(v.value), int(lvl.value)
+
+    @property
+    def counts(self):
+        c = np.zeros(3, np.uint64)
+        lib().orc_count_nodes(self._h, c.ctypes.data)
+        return tuple(int(x) for x in c)
+
+    def compute_sdf(self) -> None:
+        lib().orc_compute_sdf(self._h)
+
+    def masks(self) -> dict:
+        n5, n4, n3 = self.counts
+        out = {"kids5": np.zeros(n5 * 1024, np.uint32), "vals5": np.zeros(n5 * 1024, np.uint32),
+               "kids4": np.zeros(n4 * 128, np.uint32), "vals4": np.zeros(n4 * 128, np.uint32),
+               "vals3": np.zeros(n3 * 16, np.uint32), "origins": np.zeros((n5, 4), np.int32)}
+        lib().orc_masks(self._h, *(out[k].ctypes.data for k in ("kids5", "vals5", "kids4", "vals4", "vals3", "origins")))
+        return out
+
+    def atlas(self):
+        side = np.zeros(3, np.uint32)
+        lib().orc_atlas(self._h, side.ctypes.data, None, None, None)
+        a = [np.zeros(int(s) ** 3, np.uint32) for s in side]
+        lib().orc_atlas(self._h, side.ctypes.data, a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data)
+        return a, [int(s) for s in side]
+
+    def view(self) -> dict:
+        """compute_sdf() then the flattened view (masks, origins, atlases)."""
+        self.compute_sdf()
+        v = self.masks()
+        a, s = self.atlas()
+        v["atlas"] = a
+        v["dims"] = [(x, x, x) for x in s]
+        return v
+
+
+def state_build(eye, target, up, aspect, fovy, width, mode, show_345, sun_dir, sun_color, intensity) -> bytes:
+    f3 = C.c_float * 3
+    out = C.create_string_buffer(256)
+    lib().orc_state_build(f3(*eye), f3(*target), f3(*up), aspect, fovy, width, mode, (C.c_uint32 * 3)(*show_345),
+                          f3(*sun_dir), f3(*sun_color), intensity, out)
+    return out.raw
+
+
+def _view_struct(v: dict):
+    keep = {k: np.ascontiguousarray(v[k], np.uint32) for k in ("kids5", "vals5", "kids4", "vals4", "vals3")}
+    org = np.ascontiguousarray(v["origins"], np.int32).reshape(-1, 4)
+    atl = [np.ascontiguousarray(a, np.uint32) for a in v["atlas"]]
+    s = orc_view()
+    for k, a in keep.items():
+        setattr(s, k, a.ctypes.data)
+    s.origins = org.ctypes.data
+    s.n5, s.n4, s.n3 = keep["kids5"].size // 1024, keep["kids4"].size // 128, keep["vals3"].size // 16
+    for i in range(3):
+        s.atlas[i] = atl[i].ctypes.data
+        for j in range(3):
+            s.dims[i][j] = int(v["dims"][i][j])
+    return s, (keep, org, atl)
+
+
+def render(v: dict, state: bytes, width: int, height: int, nthreads: int = 1, hits: bool = True,
+           stats: bool = False, tiles=None):
+    """Run the oracle's raycast pass. Returns (rgba[h,w,4] u8, hits[h,w] or None, stats[h,w] or None)."""
+    s, keep = _view_struct(v)
+    rgba = np.zeros((height, width, 4), np.uint8)
+    h = np.zeros((height, width), HIT_DTYPE) if hits else None
+    st = np.zeros((height, width), STATS_DTYPE) if stats else None
+    sb = C.create_string_buffer(bytes(state), 256)
+    if tiles is None:
+        rc = lib().orc_render(C.byref(s), sb, width, height, rgba.ctypes.data,
+                              None if h is None else h.ctypes.data, None if st is None else st.ctypes.data, nthreads)
+    else:
+        rc = lib().orc_render_tiles(C.byref(s), sb, width, height, tiles[0], tiles[1], rgba.ctypes.data,
+                                    None if h is None else h.ctypes.data, None if st is None else st.ctypes.data,
+                                    nthreads)
+    if rc != 0:
+        raise RuntimeError(f"orc_render failed: {rc}")
+    del keep
+    return rgba, h, st

@@ -1,0 +1,36 @@
+import os
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the sm_103a kernels)")
+
+
+@pytest.fixture(scope="session", autouse=True)
+def built_libraries():
+    """Build libwoxel_gb300.so and the oracle once per session (no-op when up to date)."""
+    from woxel_gb300 import build as b
+
+    b.build()
+    b.build_oracle()
+    yield
+
+
+@pytest.fixture(scope="session")
+def cuda_ctx():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.fail("GPU test selected but CUDA is not available")
+    import woxel_gb300 as wx
+
+    ctx = wx.Context(int(os.environ.get("WX_TEST_DEVICE", "0")))
+    yield ctx
+    ctx.close()

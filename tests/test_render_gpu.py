@@ -1,0 +1,123 @@
+"""GPU parity: the sm_103a raycast kernel (through the C ABI) against the CPU oracle."""
+import numpy as np
+import pytest
+
+import woxel_gb300 as wx
+from parity import compare, dispatch_mask, gpu_render, oracle_render
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sphere64(cuda_ctx):
+    topo = wx.Topology.sphere((0, 0, 0), 64.0, 3.0)
+    view = topo.view()
+    return topo, view, cuda_ctx.build_grid(topo)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4])
+def test_sphere_640x480_all_modes(cuda_ctx, sphere64, mode):
+    """Config 1: sphere r=64 at the origin, band 3, camera (0,0,200) -> origin, 60 deg, 640x480."""
+    _, view, grid = sphere64
+    st = wx.state_build(eye=(0, 0, 200), target=(0, 0, 0), aspect=640 / 480, fovy=60.0, width=640.0, mode=mode)
+    rg, hg = gpu_render(cuda_ctx, grid, st, 640, 480)
+    ro, ho = oracle_render(view, st, 640, 480)
+    s = compare(rg, hg, ro, ho, label=f"mode{mode}")
+    assert s["rgba_exact"] and s["t_exact"]
+    assert (wx.hit_fields(hg)["state"] == 0).sum() > 50000  # the sphere is in view
+
+
+def test_show_345_grid_tint(cuda_ctx, sphere64):
+    _, view, grid = sphere64
+    st = wx.state_build(eye=(30, 90, 150), target=(0, 0, 0), aspect=1.0, fovy=50.0, width=256.0, mode=1,
+                        show_345=(1, 1, 1))
+    rg, hg = gpu_render(cuda_ctx, grid, st, 256, 256)
+    ro, ho = oracle_render(view, st, 256, 256)
+    compare(rg, hg, ro, ho, label="show345")
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_random_sparse_grids(cuda_ctx, seed):
+    rng = np.random.default_rng(seed)
+    ijk = rng.integers(-400, 400, size=(3000, 3)).astype(np.int32)
+    topo = wx.Topology.from_voxels(ijk)
+    view = topo.view()
+    grid = cuda_ctx.build_grid(topo)
+    eye = tuple(float(x) for x in rng.uniform(-700, 700, 3))
+    for mode in (0, 3):
+        st = wx.state_build(eye=eye, target=(0, 0, 0), aspect=1.5, fovy=70.0, width=192.0, mode=mode)
+        rg, hg = gpu_render(cuda_ctx, grid, st, 192, 128)
+        ro, ho = oracle_render(view, st, 192, 128)
+        compare(rg, hg, ro, ho, label=f"rand{seed}/mode{mode}")
+
+
+def test_dropin_view_upload_equals_native_build(cuda_ctx):
+    """wx_grid_upload (Rust-side view) and wx_grid_build (native SDF) render identically."""
+    rng = np.random.default_rng(11)
+    ijk = rng.integers(-150, 150, size=(5000, 3)).astype(np.int32)
+    topo = wx.Topology.from_voxels(ijk)
+    view = topo.view(value_texel=0x40400000)  # value texels carry f32 bits, as in the reference
+    g1 = cuda_ctx.build_grid(topo)
+    g2 = cuda_ctx.upload_view(view)
+    assert g1.info["n3"] == g2.info["n3"] and g1.info["active_voxels"] == g2.info["active_voxels"]
+    st = wx.state_build(eye=(200, 130, -260), target=(0, 0, 0), aspect=1.0, fovy=60.0, width=160.0, mode=3)
+    r1, h1 = gpu_render(cuda_ctx, g1, st, 160, 160)
+    r2, h2 = gpu_render(cuda_ctx, g2, st, 160, 160)
+    np.testing.assert_array_equal(r1, r2)
+    np.testing.assert_array_equal(h1.view(np.uint8), h2.view(np.uint8))
+    ro, ho = oracle_render(view, st, 160, 160)
+    compare(r1, h1, ro, ho, label="dropin")
+
+
+def test_host_buffers_match_device_buffers(cuda_ctx, sphere64):
+    _, view, grid = sphere64
+    st = wx.state_build(eye=(100, 40, 120), target=(0, 0, 0), aspect=4 / 3, fovy=60.0, width=320.0, mode=3)
+    rd, hd = gpu_render(cuda_ctx, grid, st, 320, 240)
+    rh, hh = gpu_render(cuda_ctx, grid, st, 320, 240, host=True)
+    np.testing.assert_array_equal(rd, rh)
+    np.testing.assert_array_equal(hd.view(np.uint8), hh.view(np.uint8))
+
+
+def test_ragged_resolution_leaves_border_untouched(cuda_ctx, sphere64):
+    """Dispatch covers 8*floor(w/8) x 4*floor(h/4) pixels (wgpu_context.rs:281); the rest is not written."""
+    _, view, grid = sphere64
+    w, h = 103, 37
+    st = wx.state_build(eye=(0, 0, 200), target=(0, 0, 0), aspect=w / h, fovy=60.0, width=float(w), mode=0)
+    rgba = np.full((h, w, 4), 7, np.uint8)
+    hits = np.zeros((h, w), wx.HIT_DTYPE)
+    cuda_ctx.render(grid, st, w, h, rgba, hits)
+    import torch
+
+    torch.cuda.synchronize()
+    m = dispatch_mask(w, h)
+    assert (rgba[~m] == 7).all()
+    ro, ho = oracle_render(view, st, w, h)
+    compare(rgba, hits, ro, ho, where=m, label="ragged")
+
+
+def test_edge_cameras(cuda_ctx, sphere64):
+    """Eye inside the band (hit at i=0, zero mask), far outside the +-4096 bound, on node boundaries."""
+    _, view, grid = sphere64
+    for eye, target in [((64.0, 0.5, 0.5), (0, 0, 0)),       # inside an active voxel
+                        ((9000.0, 10.0, 5.0), (0, 0, 0)),    # beyond the bound: state 1 at step 0
+                        ((0.0, 0.0, 128.0), (0, 0, 0)),      # on N4/N5 boundaries
+                        ((-128.0, 4096.0, -8.0), (0, 0, 0))]:
+        for mode in (0, 3, 4):
+            st = wx.state_build(eye=eye, target=target, aspect=1.0, fovy=75.0, width=64.0, mode=mode)
+            rg, hg = gpu_render(cuda_ctx, grid, st, 64, 64)
+            ro, ho = oracle_render(view, st, 64, 64)
+            compare(rg, hg, ro, ho, label=f"eye{eye}/mode{mode}")
+
+
+def test_empty_grid(cuda_ctx):
+    topo = wx.Topology.from_voxels(np.zeros((0, 3), np.int32))
+    assert topo.counts == (0, 0, 0)
+    grid = cuda_ctx.build_grid(topo)
+    view = {"kids5": np.zeros(0, np.uint32), "vals5": np.zeros(0, np.uint32), "kids4": np.zeros(0, np.uint32),
+            "vals4": np.zeros(0, np.uint32), "vals3": np.zeros(0, np.uint32), "origins": np.zeros((0, 4), np.int32),
+            "atlas": [np.zeros(1, np.uint32)] * 3, "dims": [(0, 0, 0)] * 3}
+    st = wx.state_build(eye=(0, 0, 200), target=(0, 0, 0), aspect=1.0, fovy=60.0, width=32.0, mode=3)
+    rg, hg = gpu_render(cuda_ctx, grid, st, 32, 32)
+    ro, ho = oracle_render(view, st, 32, 32)
+    compare(rg, hg, ro, ho, label="empty")
+    assert (wx.hit_fields(hg)["state"] == 1).all()

@@ -1,0 +1,255 @@
+"""woxel_gb300 — GB300 (sm_103a) primary-ray pass for woxel's VDB345 grids.
+
+Host-side mirror of the reference's raycast-pass interface: a grid is
+uploaded once (WgpuContext::new / change_vdb_model, src/render/wgpu_context.rs:
+101-159, 506-573), then every frame takes the 256-byte ComputeState uniform
+(src/render/gpu_types/compute_state.rs:9-29) and produces RGBA8 plus an
+optional hit buffer (the compute pass of src/render/wgpu_context.rs:270-282).
+All work runs in libwoxel_gb300.so through its C ABI (include/woxel_gb300.h);
+there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+
+from ._ffi import (WX_OK, WxError, check, lib, wx_grid_info, wx_hit, wx_state_uniform,  # noqa: F401
+                   wx_vdb345_view)
+
+HIT_DTYPE = np.dtype([("p", "<f4", (3,)), ("t", "<f4"), ("node", "<u4"), ("info", "<u4"),
+                      ("shadow", "<u4"), ("reserved", "<u4")])
+assert HIT_DTYPE.itemsize == 32
+
+MODE_GRAY, MODE_RGB, MODE_RAY, MODE_DIFFUSE, MODE_GLOSSY = 0, 1, 2, 3, 4
+
+
+def _ptr(a) -> Optional[int]:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):  # torch.Tensor
+        return a.data_ptr()
+    return int(a)
+
+
+def hit_fields(hits: np.ndarray) -> dict:
+    """Decode wx_hit records: state, level, mask, steps, node, ijk = floor(p), t, shadow."""
+    info = hits["info"]
+    return {
+        "state": info & 3, "level": (info >> 2) & 3, "mask": (info >> 4) & 7, "steps": (info >> 8) & 0x7FF,
+        "node": hits["node"], "ijk": np.floor(hits["p"]).astype(np.int32), "t": hits["t"],
+        "p": hits["p"], "shadow": hits["shadow"],
+    }
+
+
+# --------------------------------------------------------------------------
+# Topology (host): node structure of a VDB345 grid in DFS order.
+# --------------------------------------------------------------------------
+class Topology:
+    def __init__(self, handle: int):
+        self._h = C.c_void_p(handle)
+
+    @staticmethod
+    def _make(fn, *args) -> "Topology":
+        out = C.c_void_p()
+        check(fn(*args, C.byref(out)))
+        return Topology(out.value)
+
+    @classmethod
+    def sphere(cls, center=(0.0, 0.0, 0.0), radius=64.0, band=3.0) -> "Topology":
+        return cls._make(lib().wx_gen_sphere, *map(float, center), float(radius), float(band))
+
+    @classmethod
+    def spheres(cls, count=2000, rmin=4.0, rmax=40.0, lo=-1024.0, hi=1024.0, band=3.0, seed=2) -> "Topology":
+        return cls._make(lib().wx_gen_spheres, count, rmin, rmax, lo, hi, band, seed)
+
+    @classmethod
+    def noise_leaves(cls, lo=-2048, extent=4096, occupancy=0.02, p_voxel=0.5, seed=3, nthreads=0) -> "Topology":
+        return cls._make(lib().wx_gen_noise_leaves, lo, extent, occupancy, p_voxel, seed, nthreads)
+
+    @classmethod
+    def from_voxels(cls, ijk) -> "Topology":
+        a = np.ascontiguousarray(ijk, dtype=np.int32).reshape(-1, 3)
+        return cls._make(lib().wx_topology_from_voxels, a.ctypes.data, a.shape[0])
+
+    @classmethod
+    def from_leaves(cls, origins, masks) -> "Topology":
+        o = np.ascontiguousarray(origins, dtype=np.int32).reshape(-1, 3)
+        m = np.ascontiguousarray(masks, dtype=np.uint64).reshape(-1, 8)
+        return cls._make(lib().wx_topology_from_leaves, o.ctypes.data, m.ctypes.data, o.shape[0])
+
+    @classmethod
+    def from_masks(cls, m: dict) -> "Topology":
+        arrs = {k: np.ascontiguousarray(m[k], dtype=np.uint32) for k in ("kids5", "vals5", "kids4", "vals4", "vals3")}
+        org = np.ascontiguousarray(m["origins"], dtype=np.int32)
+        stride = org.shape[1] if org.ndim == 2 else 4
+        n5, n4, n3 = arrs["kids5"].size // 1024, arrs["kids4"].size // 128, arrs["vals3"].size // 16
+        return cls._make(lib().wx_topology_from_masks, arrs["kids5"].ctypes.data, arrs["vals5"].ctypes.data, n5,
+                         arrs["kids4"].ctypes.data, arrs["vals4"].ctypes.data, n4, arrs["vals3"].ctypes.data, n3,
+                         org.ctypes.data, stride)
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            lib().wx_topology_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def counts(self) -> tuple:
+        c = (C.c_uint64 * 3)()
+        check(lib().wx_topology_counts(self._h, c))
+        return int(c[0]), int(c[1]), int(c[2])
+
+    @property
+    def active_voxels(self) -> int:
+        return int(lib().wx_topology_active_voxels(self._h))
+
+    def masks(self) -> dict:
+        """masks()/origins() of the reference (src/vdb/vdb345.rs:108-161)."""
+        n5, n4, n3 = self.counts
+        out = {"kids5": np.zeros(n5 * 1024, np.uint32), "vals5": np.zeros(n5 * 1024, np.uint32),
+               "kids4": np.zeros(n4 * 128, np.uint32), "vals4": np.zeros(n4 * 128, np.uint32),
+               "vals3": np.zeros(n3 * 16, np.uint32), "origins": np.zeros((n5, 4), np.int32)}
+        check(lib().wx_topology_masks(self._h, *(out[k].ctypes.data for k in
+                                                 ("kids5", "vals5", "kids4", "vals4", "vals3", "origins"))))
+        return out
+
+    def sdf(self, nthreads: int = 0) -> None:
+        check(lib().wx_topology_sdf(self._h, nthreads))
+
+    def atlas(self, value_texel: int = 1) -> tuple:
+        """atlas() in the uploaded texture layout: three flat u32 arrays and their cube sides."""
+        side = (C.c_uint32 * 3)()
+        check(lib().wx_topology_atlas(self._h, side, None, None, None, 0))
+        s = [int(x) for x in side]
+        a = [np.zeros(x ** 3, np.uint32) for x in s]
+        check(lib().wx_topology_atlas(self._h, side, a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data,
+                                      value_texel))
+        return a, s
+
+    def view(self, value_texel: int = 1) -> dict:
+        """The flattened reference view (masks + origins + atlases), computing the SDF first."""
+        self.sdf()
+        v = self.masks()
+        a, s = self.atlas(value_texel)
+        v["atlas"] = a
+        v["dims"] = [(x, x, x) for x in s]
+        return v
+
+
+# --------------------------------------------------------------------------
+# Uniform and cameras
+# --------------------------------------------------------------------------
+def sun_default() -> tuple:
+    d, c, i = (C.c_float * 3)(), (C.c_float * 3)(), C.c_float()
+    lib().wx_sun_default(d, c, C.byref(i))
+    return tuple(d), tuple(c), i.value
+
+
+def state_build(eye, target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), aspect=4.0 / 3.0, fovy=60.0, width=640.0,
+                mode=MODE_DIFFUSE, show_345=(0, 0, 0), sun=None) -> wx_state_uniform:
+    sd, sc, si = sun if sun is not None else sun_default()
+    f3 = C.c_float * 3
+    out = wx_state_uniform()
+    check(lib().wx_state_build(f3(*eye), f3(*target), f3(*up), aspect, fovy, width, mode,
+                               (C.c_uint32 * 3)(*show_345), f3(*sd), f3(*sc), si, C.byref(out)))
+    return out
+
+
+def state_bytes(s: wx_state_uniform) -> bytes:
+    return C.string_at(C.addressof(s), 256)
+
+
+def state_from_bytes(b: bytes) -> wx_state_uniform:
+    s = wx_state_uniform()
+    C.memmove(C.addressof(s), b, 256)
+    return s
+
+
+def orbit_eyes(count: int, radius: float, seed: int) -> np.ndarray:
+    out = np.zeros((count, 3), np.float32)
+    check(lib().wx_orbit_eyes(count, radius, seed, out.ctypes.data))
+    return out
+
+
+# --------------------------------------------------------------------------
+# Device context and grids
+# --------------------------------------------------------------------------
+class Grid:
+    def __init__(self, ctx: "Context", handle: int):
+        self.ctx = ctx
+        self._h = C.c_void_p(handle)
+
+    @property
+    def info(self) -> dict:
+        i = wx_grid_info()
+        check(lib().wx_grid_get_info(self._h, C.byref(i)))
+        return {k: int(getattr(i, k)) for k, _ in wx_grid_info._fields_}
+
+    def release(self) -> None:
+        if self._h and self._h.value:
+            check(lib().wx_grid_release(self.ctx._h, self._h), self.ctx._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        out = C.c_void_p()
+        check(lib().wx_ctx_create(device, C.byref(out)))
+        self._h = out
+        self.device = device
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            lib().wx_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def build_grid(self, topo: Topology) -> Grid:
+        out = C.c_void_p()
+        check(lib().wx_grid_build(self._h, topo._h, C.byref(out)), self._h)
+        return Grid(self, out.value)
+
+    def upload_view(self, v: dict) -> Grid:
+        """Drop-in upload of the Rust side's flattened view (masks, origins, atlases)."""
+        keep = {k: np.ascontiguousarray(v[k], dtype=np.uint32) for k in ("kids5", "vals5", "kids4", "vals4", "vals3")}
+        org = np.ascontiguousarray(v["origins"], dtype=np.int32)
+        atl = [np.ascontiguousarray(a, dtype=np.uint32) for a in v["atlas"]]
+        view = wx_vdb345_view()
+        for k, a in keep.items():
+            setattr(view, k, a.ctypes.data)
+        view.origins = org.ctypes.data
+        view.origin_stride = org.shape[1] if org.ndim == 2 else 4
+        view.n5, view.n4, view.n3 = keep["kids5"].size // 1024, keep["kids4"].size // 128, keep["vals3"].size // 16
+        for i in range(3):
+            view.atlas[i] = atl[i].ctypes.data
+            for j in range(3):
+                view.dims[i][j] = int(v["dims"][i][j])
+        out = C.c_void_p()
+        check(lib().wx_grid_upload(self._h, C.byref(view), C.byref(out)), self._h)
+        return Grid(self, out.value)
+
+    def render(self, grid: Grid, state: wx_state_uniform, width: int, height: int, rgba, hits=None,
+               stream=None) -> None:
+        """One frame: rgba (w*h*4 bytes) and hits (w*h records) are device tensors or host arrays."""
+        check(lib().wx_render(self._h, grid._h, C.byref(state), width, height, _ptr(rgba), _ptr(hits),
+                              None if stream is None else int(stream)), self._h)

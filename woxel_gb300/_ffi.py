@@ -1,0 +1,102 @@
+"""ctypes binding of libwoxel_gb300.so (declarations mirror include/woxel_gb300.h)."""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libwoxel_gb300.so"
+
+WX_OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "unsupported",
+          5: "over memory budget", 6: "timed out", 7: "cancelled"}
+
+
+class wx_state_uniform(C.Structure):
+    _fields_ = [("view_projection", C.c_float * 16), ("camera_to_world", C.c_float * 16),
+                ("eye", C.c_float * 4), ("u", C.c_float * 4), ("mv", C.c_float * 4), ("wp", C.c_float * 4),
+                ("render_mode", C.c_uint32 * 4), ("show_345", C.c_uint32 * 4),
+                ("sun_dir", C.c_float * 4), ("sun_color", C.c_float * 4)]
+
+
+class wx_hit(C.Structure):
+    _fields_ = [("p", C.c_float * 3), ("t", C.c_float), ("node", C.c_uint32), ("info", C.c_uint32),
+                ("shadow", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class wx_vdb345_view(C.Structure):
+    _fields_ = [("kids5", C.c_void_p), ("vals5", C.c_void_p), ("kids4", C.c_void_p), ("vals4", C.c_void_p),
+                ("vals3", C.c_void_p), ("origins", C.c_void_p), ("n5", C.c_uint64), ("n4", C.c_uint64),
+                ("n3", C.c_uint64), ("origin_stride", C.c_uint32), ("atlas", C.c_void_p * 3),
+                ("dims", (C.c_uint32 * 3) * 3)]
+
+
+class wx_grid_info(C.Structure):
+    _fields_ = [("n5", C.c_uint64), ("n4", C.c_uint64), ("n3", C.c_uint64), ("device_bytes", C.c_uint64),
+                ("active_voxels", C.c_uint64)]
+
+
+assert C.sizeof(wx_state_uniform) == 256
+assert C.sizeof(wx_hit) == 32
+
+P = C.c_void_p
+U32, U64, I32, F32, INT = C.c_uint32, C.c_uint64, C.c_int32, C.c_float, C.c_int
+
+# name -> (restype, argtypes); every symbol the header declares.
+SIGNATURES = {
+    "wx_status_string": (C.c_char_p, [INT]),
+    "wx_thread_last_error": (C.c_char_p, []),
+    "wx_version": (C.c_char_p, []),
+    "wx_ctx_create": (INT, [INT, C.POINTER(P)]),
+    "wx_ctx_destroy": (INT, [P]),
+    "wx_last_error": (C.c_char_p, [P]),
+    "wx_grid_upload": (INT, [P, C.POINTER(wx_vdb345_view), C.POINTER(P)]),
+    "wx_grid_build": (INT, [P, P, C.POINTER(P)]),
+    "wx_grid_release": (INT, [P, P]),
+    "wx_grid_get_info": (INT, [P, C.POINTER(wx_grid_info)]),
+    "wx_render": (INT, [P, P, C.POINTER(wx_state_uniform), U32, U32, P, P, P]),
+    "wx_state_build": (INT, [P, P, P, F32, F32, F32, U32, P, P, P, F32, C.POINTER(wx_state_uniform)]),
+    "wx_sun_default": (None, [P, P, P]),
+    "wx_topology_from_masks": (INT, [P, P, U64, P, P, U64, P, U64, P, U32, C.POINTER(P)]),
+    "wx_topology_from_voxels": (INT, [P, U64, C.POINTER(P)]),
+    "wx_topology_from_leaves": (INT, [P, P, U64, C.POINTER(P)]),
+    "wx_topology_free": (None, [P]),
+    "wx_topology_counts": (INT, [P, P]),
+    "wx_topology_active_voxels": (U64, [P]),
+    "wx_topology_masks": (INT, [P, P, P, P, P, P, P]),
+    "wx_topology_sdf": (INT, [P, INT]),
+    "wx_topology_atlas": (INT, [P, P, P, P, P, U32]),
+    "wx_gen_sphere": (INT, [F32, F32, F32, F32, F32, C.POINTER(P)]),
+    "wx_gen_spheres": (INT, [U32, F32, F32, F32, F32, F32, U64, C.POINTER(P)]),
+    "wx_gen_noise_leaves": (INT, [I32, U32, C.c_double, C.c_double, U64, INT, C.POINTER(P)]),
+    "wx_orbit_eyes": (INT, [U32, F32, U64, P]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libwoxel_gb300.so; raises if it has not been built (no fallback exists)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: run `python -m woxel_gb300.build` (there is no CPU fallback)")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class WxError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def check(status: int, ctx=None) -> None:
+    if status != WX_OK:
+        L = lib()
+        msg = (L.wx_last_error(ctx) if ctx else L.wx_thread_last_error()) or b""
+        raise WxError(status, msg.decode(errors="replace"))

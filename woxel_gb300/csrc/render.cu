@@ -1,0 +1,408 @@
+// render.cu — device node pools, the plain per-frame raycast kernel and the
+// C ABI around them (context, grid upload/build, render).
+//
+// Device layout (uploaded once per grid, immutable afterwards):
+//   o5     n5 x int4         N5 origins (root keys) in DFS order
+//   slot5  n5 x 32768 u32    per N4-sized slot: child flag|N4 index, or skip distance
+//   slot4  n4 x  4096 u32    per N3-sized slot: child flag|N3 index, or skip distance
+//   slot3  n3 x   512 u32    per voxel: skip distance, 0 for an active voxel
+// A slot word folds the reference's three reads per level (child-mask word,
+// value-mask word, atlas texel; raycast.comp.wgsl:422-429, :453-461,
+// :483-489) into one 4-byte load that decides hit / descend / skip.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "wx_common.h"
+#include "wx_device.cuh"
+
+struct wx_ctx {
+    int device = 0;
+    std::string err;
+    void *stage = nullptr;  // device staging for host-memory outputs
+    size_t stage_bytes = 0;
+};
+
+struct wx_grid {
+    int device = 0;
+    void *dev = nullptr;
+    size_t bytes = 0;
+    wxd::DevGrid g{};
+    wx_grid_info info{};
+};
+
+namespace {
+
+int fail(wx_ctx *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->err = msg;
+    wx::set_thread_error(msg);
+    return code;
+}
+int cuda_fail(wx_ctx *ctx, cudaError_t e, const char *what) {
+    return fail(ctx, e == cudaErrorMemoryAllocation ? WX_ERR_OOM : WX_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define WX_CUDA(ctx, call)                                   \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+constexpr int kWarpsPerBlock = 4;
+
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    k_render_plain(wxd::DevGrid g, wx_state_uniform s, uint32_t width, uint32_t tiles_x, uint32_t ntiles,
+                   uint32_t *__restrict__ rgba, wx_hit *__restrict__ hits) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (tile >= ntiles) return;
+    // One warp = one 8x4 pixel tile, the reference's workgroup (raycast.comp.wgsl:60).
+    const uint32_t gx = (tile % tiles_x) * 8u + (lane & 7u);
+    const uint32_t gy = (tile / tiles_x) * 4u + (lane >> 3);
+    uint32_t c;
+    wx_hit rec;
+    wxd::shade_pixel(g, s, gx, gy, c, rec);
+    const size_t pix = (size_t)gy * width + gx;
+    rgba[pix] = c;
+    if (hits) {
+        uint4 *h = reinterpret_cast<uint4 *>(hits + pix);
+        h[0] = make_uint4(__float_as_uint(rec.p[0]), __float_as_uint(rec.p[1]), __float_as_uint(rec.p[2]),
+                          __float_as_uint(rec.t));
+        h[1] = make_uint4(rec.node, rec.info, rec.shadow, 0u);
+    }
+}
+
+bool device_accessible(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Allocate one device block for the pools and fill the DevGrid pointers.
+int alloc_grid(wx_ctx *ctx, uint64_t n5, uint64_t n4, uint64_t n3, wx_grid **out) {
+    auto *gr = new (std::nothrow) wx_grid();
+    if (!gr) return fail(ctx, WX_ERR_OOM, "host allocation failed");
+    auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t b_o5 = align(std::max<uint64_t>(n5, 1) * 16), b5 = align(n5 * 32768ull * 4),
+                 b4 = align(n4 * 4096ull * 4), b3 = align(n3 * 512ull * 4);
+    gr->bytes = b_o5 + b5 + b4 + b3;
+    gr->device = ctx->device;
+    cudaError_t e = cudaMalloc(&gr->dev, gr->bytes);
+    if (e != cudaSuccess) {
+        delete gr;
+        return cuda_fail(ctx, e, "cudaMalloc(node pools)");
+    }
+    char *b = static_cast<char *>(gr->dev);
+    gr->g.o5 = reinterpret_cast<const int4 *>(b);
+    gr->g.slot5 = reinterpret_cast<const uint32_t *>(b + b_o5);
+    gr->g.slot4 = reinterpret_cast<const uint32_t *>(b + b_o5 + b5);
+    gr->g.slot3 = reinterpret_cast<const uint32_t *>(b + b_o5 + b5 + b4);
+    gr->g.n5 = (uint32_t)n5;
+    gr->info.n5 = n5;
+    gr->info.n4 = n4;
+    gr->info.n3 = n3;
+    gr->info.device_bytes = gr->bytes;
+    *out = gr;
+    return WX_OK;
+}
+
+template <class F>
+void parallel_chunks(size_t n, F f) {
+    unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (n < 4096 || nt == 1) {
+        f(0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    const size_t chunk = (n + nt - 1) / nt;
+    for (unsigned t = 0; t < nt; t++) {
+        const size_t lo = t * chunk, hi = std::min(n, lo + chunk);
+        if (lo < hi) th.emplace_back([=] { f(lo, hi); });
+    }
+    for (auto &x : th) x.join();
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *wx_status_string(int status) {
+    switch (status) {
+        case WX_OK: return "ok";
+        case WX_ERR_INVALID: return "invalid argument";
+        case WX_ERR_CUDA: return "CUDA error";
+        case WX_ERR_OOM: return "out of memory";
+        case WX_ERR_UNSUPPORTED: return "unsupported";
+        case WX_ERR_BUDGET: return "over memory budget";
+        case WX_ERR_TIMEOUT: return "timed out";
+        case WX_ERR_CANCELLED: return "cancelled";
+        default: return "unknown status";
+    }
+}
+
+int wx_ctx_create(int device, wx_ctx **out) {
+    if (!out) return fail(nullptr, WX_ERR_INVALID, "wx_ctx_create: out is NULL");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDeviceCount");
+    if (device < 0 || device >= n) return fail(nullptr, WX_ERR_INVALID, "wx_ctx_create: no such device");
+    WX_CUDA(nullptr, cudaSetDevice(device));
+    WX_CUDA(nullptr, cudaFree(nullptr));
+    auto *c = new (std::nothrow) wx_ctx();
+    if (!c) return fail(nullptr, WX_ERR_OOM, "host allocation failed");
+    c->device = device;
+    *out = c;
+    return WX_OK;
+}
+
+int wx_ctx_destroy(wx_ctx *ctx) {
+    if (!ctx) return WX_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stage) cudaFree(ctx->stage);
+    delete ctx;
+    return WX_OK;
+}
+
+const char *wx_last_error(const wx_ctx *ctx) { return ctx ? ctx->err.c_str() : wx_thread_last_error(); }
+
+int wx_grid_build(wx_ctx *ctx, wx_topology *t, wx_grid **out) {
+    if (!ctx || !t || !out) return fail(ctx, WX_ERR_INVALID, "wx_grid_build: null argument");
+    WX_CUDA(ctx, cudaSetDevice(ctx->device));
+    int rc = wx_topology_sdf(t, 0);
+    if (rc != WX_OK) return fail(ctx, rc, wx_thread_last_error());
+    const uint64_t n5 = t->n5(), n4 = t->n4(), n3 = t->n3();
+    if (n4 >= wx::kChildFlag || n3 >= wx::kChildFlag)
+        return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_build: more than 2^31 nodes in a level");
+    std::vector<uint32_t> s5, s4;
+    std::vector<int4> o5(std::max<uint64_t>(n5, 1));
+    try {
+        s5.resize(n5 * wx::kN5Slots);
+        s4.resize(n4 * wx::kN4Slots);
+    } catch (...) {
+        return fail(ctx, WX_ERR_OOM, "wx_grid_build: host allocation failed");
+    }
+    bool too_far = false;
+    for (uint64_t i = 0; i < n5; i++) {
+        o5[i] = make_int4(t->o5[i][0], t->o5[i][1], t->o5[i][2], 0);
+        uint32_t next = t->first4[i];
+        for (uint32_t s = 0; s < wx::kN5Slots; s++) {
+            const bool kid = wx::test_bit(&t->kid5[i * wx::kN5Words], s);
+            const bool val = wx::test_bit(&t->val5[i * wx::kN5Words], s);
+            const uint32_t d = t->d5[i * wx::kN5Slots + s];
+            if (kid) {
+                const uint32_t c = next++;
+                s5[i * wx::kN5Slots + s] = val ? 0u : (wx::kChildFlag | c);
+            } else {
+                too_far |= !val && d >= wx::kChildFlag;
+                s5[i * wx::kN5Slots + s] = val ? 0u : d;
+            }
+        }
+    }
+    for (uint64_t j = 0; j < n4; j++) {
+        uint32_t next = t->first3[j];
+        for (uint32_t s = 0; s < wx::kN4Slots; s++) {
+            const bool kid = wx::test_bit(&t->kid4[j * wx::kN4Words], s);
+            const bool val = wx::test_bit(&t->val4[j * wx::kN4Words], s);
+            const uint32_t d = t->d4[j * wx::kN4Slots + s];
+            if (kid) {
+                const uint32_t c = next++;
+                s4[j * wx::kN4Slots + s] = val ? 0u : (wx::kChildFlag | c);
+            } else {
+                too_far |= !val && d >= wx::kChildFlag;
+                s4[j * wx::kN4Slots + s] = val ? 0u : d;
+            }
+        }
+    }
+    if (too_far) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_build: tile distance >= 2^31");
+    wx_grid *gr = nullptr;
+    rc = alloc_grid(ctx, n5, n4, n3, &gr);
+    if (rc != WX_OK) return rc;
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess && n5) e = cudaMemcpy((void *)gr->g.o5, o5.data(), n5 * 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n5) e = cudaMemcpy((void *)gr->g.slot5, s5.data(), s5.size() * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n4) e = cudaMemcpy((void *)gr->g.slot4, s4.data(), s4.size() * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n3)
+        e = cudaMemcpy((void *)gr->g.slot3, t->slot3.data(), n3 * 512ull * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(gr->dev);
+        delete gr;
+        return cuda_fail(ctx, e, "cudaMemcpy(node pools)");
+    }
+    gr->info.active_voxels = wx_topology_active_voxels(t);
+    *out = gr;
+    return WX_OK;
+}
+
+int wx_grid_upload(wx_ctx *ctx, const wx_vdb345_view *v, wx_grid **out) {
+    if (!ctx || !v || !out) return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: null argument");
+    if (v->origin_stride < 3) return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: origin_stride < 3");
+    const uint64_t n5 = v->n5, n4 = v->n4, n3 = v->n3;
+    if ((n5 && (!v->kids5 || !v->vals5 || !v->origins || !v->atlas[0])) ||
+        (n4 && (!v->kids4 || !v->vals4 || !v->atlas[1])) || (n3 && (!v->vals3 || !v->atlas[2])))
+        return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: missing mask/atlas arrays");
+    if (n4 >= wx::kChildFlag || n3 >= wx::kChildFlag || n5 >= wx::kChildFlag)
+        return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_upload: more than 2^31 nodes in a level");
+    WX_CUDA(ctx, cudaSetDevice(ctx->device));
+    // Atlas block placement as the shader computes it: dim = textureDimensions
+    // (.y for N5, .x for N4/N3) >> log2(node dim); block (idx%d, (idx/d)%d, idx/d^2).
+    const uint32_t d5 = v->dims[0][1] >> 5, d4 = v->dims[1][0] >> 4, d3 = v->dims[2][0] >> 3;
+    auto block_ok = [&](int lvl, uint64_t n, uint32_t d, uint32_t nd) {
+        if (n == 0) return true;
+        if (d == 0) return false;
+        const uint64_t dd = (uint64_t)d * d;
+        const uint64_t need_x = nd * std::min<uint64_t>(n, d), need_y = nd * std::min<uint64_t>((n + d - 1) / d, d),
+                       need_z = nd * ((n + dd - 1) / dd);
+        return need_x <= v->dims[lvl][0] && need_y <= v->dims[lvl][1] && need_z <= v->dims[lvl][2];
+    };
+    if (!block_ok(0, n5, d5, 32) || !block_ok(1, n4, d4, 16) || !block_ok(2, n3, d3, 8))
+        return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: atlas dimensions too small for the node counts");
+    auto texel = [&](int lvl, uint64_t idx, uint32_t d, uint32_t nd, uint32_t cx, uint32_t cy, uint32_t cz) {
+        const uint64_t x = nd * (idx % d) + cx, y = nd * ((idx / d) % d) + cy, z = nd * (idx / ((uint64_t)d * d)) + cz;
+        return v->atlas[lvl][(z * v->dims[lvl][1] + y) * v->dims[lvl][0] + x];
+    };
+    std::vector<uint32_t> s5, s4, s3;
+    std::vector<int4> o5(std::max<uint64_t>(n5, 1));
+    try {
+        s5.resize(n5 * wx::kN5Slots);
+        s4.resize(n4 * wx::kN4Slots);
+        s3.resize(n3 * wx::kN3Slots);
+    } catch (...) {
+        return fail(ctx, WX_ERR_OOM, "wx_grid_upload: host allocation failed");
+    }
+    std::atomic<int> bad{0};
+    for (uint64_t i = 0; i < n5; i++) {
+        const int32_t *o = v->origins + i * v->origin_stride;
+        o5[i] = make_int4(o[0], o[1], o[2], 0);
+    }
+    parallel_chunks(n5, [&](size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; i++)
+            for (uint32_t s = 0; s < wx::kN5Slots; s++) {
+                const uint32_t w = s >> 5, b = 1u << (s & 31);
+                const bool kid = v->kids5[i * 1024 + w] & b, val = v->vals5[i * 1024 + w] & b;
+                uint32_t c[3];
+                wx::offset_child(s, 5, c);
+                const uint32_t tx = texel(0, i, d5, 32, c[0], c[1], c[2]);
+                uint32_t word;
+                if (val) word = 0;
+                else if (kid) { word = wx::kChildFlag | tx; if (tx >= n4) bad = 1; }
+                else { word = tx; if (tx >= wx::kChildFlag) bad = 2; }
+                s5[i * wx::kN5Slots + s] = word;
+            }
+    });
+    parallel_chunks(n4, [&](size_t lo, size_t hi) {
+        for (size_t j = lo; j < hi; j++)
+            for (uint32_t s = 0; s < wx::kN4Slots; s++) {
+                const uint32_t w = s >> 5, b = 1u << (s & 31);
+                const bool kid = v->kids4[j * 128 + w] & b, val = v->vals4[j * 128 + w] & b;
+                uint32_t c[3];
+                wx::offset_child(s, 4, c);
+                const uint32_t tx = texel(1, j, d4, 16, c[0], c[1], c[2]);
+                uint32_t word;
+                if (val) word = 0;
+                else if (kid) { word = wx::kChildFlag | tx; if (tx >= n3) bad = 1; }
+                else { word = tx; if (tx >= wx::kChildFlag) bad = 2; }
+                s4[j * wx::kN4Slots + s] = word;
+            }
+    });
+    parallel_chunks(n3, [&](size_t lo, size_t hi) {
+        for (size_t k = lo; k < hi; k++)
+            for (uint32_t s = 0; s < wx::kN3Slots; s++) {
+                const bool val = v->vals3[k * 16 + (s >> 5)] & (1u << (s & 31));
+                uint32_t c[3];
+                wx::offset_child(s, 3, c);
+                s3[k * wx::kN3Slots + s] = val ? 0u : texel(2, k, d3, 8, c[0], c[1], c[2]);
+            }
+    });
+    if (bad == 1) return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: child index in atlas out of range");
+    if (bad == 2) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_upload: internal tile distance >= 2^31");
+    wx_grid *gr = nullptr;
+    int rc = alloc_grid(ctx, n5, n4, n3, &gr);
+    if (rc != WX_OK) return rc;
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess && n5) e = cudaMemcpy((void *)gr->g.o5, o5.data(), n5 * 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n5) e = cudaMemcpy((void *)gr->g.slot5, s5.data(), s5.size() * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n4) e = cudaMemcpy((void *)gr->g.slot4, s4.data(), s4.size() * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n3) e = cudaMemcpy((void *)gr->g.slot3, s3.data(), s3.size() * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(gr->dev);
+        delete gr;
+        return cuda_fail(ctx, e, "cudaMemcpy(node pools)");
+    }
+    uint64_t act = 0;
+    for (uint64_t w = 0; w < n3 * 16; w++) act += (uint64_t)__builtin_popcount(v->vals3[w]);
+    gr->info.active_voxels = act;
+    *out = gr;
+    return WX_OK;
+}
+
+int wx_grid_release(wx_ctx *ctx, wx_grid *grid) {
+    if (!grid) return WX_OK;
+    cudaSetDevice(grid->device);
+    cudaError_t e = cudaFree(grid->dev);
+    delete grid;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaFree(node pools)");
+    return WX_OK;
+}
+
+int wx_grid_get_info(const wx_grid *grid, wx_grid_info *out) {
+    if (!grid || !out) return WX_ERR_INVALID;
+    *out = grid->info;
+    return WX_OK;
+}
+
+int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, uint32_t width,
+              uint32_t height, uint8_t *rgba8, wx_hit *hits, void *stream) {
+    if (!ctx || !grid || !state || !rgba8) return fail(ctx, WX_ERR_INVALID, "wx_render: null argument");
+    if (grid->device != ctx->device) return fail(ctx, WX_ERR_INVALID, "wx_render: grid is on another device");
+    WX_CUDA(ctx, cudaSetDevice(ctx->device));
+    const uint32_t tiles_x = width / 8, tiles_y = height / 4;
+    const uint64_t ntiles = (uint64_t)tiles_x * tiles_y;
+    if (ntiles == 0) return WX_OK;
+    if (ntiles > (1ull << 31)) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_render: frame too large");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const bool dev_rgba = device_accessible(rgba8);
+    const bool dev_hits = hits ? device_accessible(hits) : true;
+    const size_t npix = (size_t)width * height;
+    uint32_t *out_rgba = reinterpret_cast<uint32_t *>(rgba8);
+    wx_hit *out_hits = hits;
+    if (!dev_rgba || !dev_hits) {
+        const size_t need = npix * 4 + (hits ? npix * sizeof(wx_hit) + 256 : 0);
+        if (need > ctx->stage_bytes) {
+            if (ctx->stage) cudaFree(ctx->stage);
+            ctx->stage = nullptr;
+            ctx->stage_bytes = 0;
+            WX_CUDA(ctx, cudaMalloc(&ctx->stage, need));
+            ctx->stage_bytes = need;
+        }
+        char *b = static_cast<char *>(ctx->stage);
+        if (!dev_rgba) out_rgba = reinterpret_cast<uint32_t *>(b);
+        if (hits && !dev_hits) out_hits = reinterpret_cast<wx_hit *>(b + ((npix * 4 + 255) & ~(size_t)255));
+    }
+    const uint32_t blocks = (uint32_t)((ntiles + kWarpsPerBlock - 1) / kWarpsPerBlock);
+    k_render_plain<<<blocks, 32 * kWarpsPerBlock, 0, st>>>(grid->g, *state, width, tiles_x, (uint32_t)ntiles,
+                                                         out_rgba, out_hits);
+    WX_CUDA(ctx, cudaGetLastError());
+    // Copy back only the dispatched region; the rest of a host buffer is untouched.
+    if (!dev_rgba)
+        WX_CUDA(ctx, cudaMemcpy2DAsync(rgba8, (size_t)width * 4, out_rgba, (size_t)width * 4, (size_t)tiles_x * 32,
+                                       (size_t)tiles_y * 4, cudaMemcpyDeviceToHost, st));
+    if (hits && !dev_hits)
+        WX_CUDA(ctx, cudaMemcpy2DAsync(hits, (size_t)width * sizeof(wx_hit), out_hits, (size_t)width * sizeof(wx_hit),
+                                       (size_t)tiles_x * 8 * sizeof(wx_hit), (size_t)tiles_y * 4,
+                                       cudaMemcpyDeviceToHost, st));
+    return WX_OK;
+}
+
+}  // extern "C"
