@@ -1,0 +1,355 @@
+"""Benchmark: primary-ray Grays/s of the raycast pass on one GB300.
+
+Default workload (one "step"): the 2000-sphere narrow-band grid (1.0 GB of
+node pools, resident in HBM) rendered from 16 orbit cameras at 1920x1080 in
+Lambert mode (primary + shadow rays), one plain per-frame launch per camera.
+value = primary rays / device time; e2e = the same through wx_render with
+host output buffers (device->host copy of every frame inside the timed region).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference algorithm's CPU implementation (the C
+restatement of raycast.comp.wgsl in oracle/, all host threads) on a bounded
+sample of the same frames; the reference itself (Rust + wgpu) cannot run here.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+MEASURED = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def hbm_peak():
+    try:
+        d = json.loads(MEASURED.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# CPU side: the oracle (restated reference algorithm) on a bounded tile sample.
+# --------------------------------------------------------------------------
+def sample_tiles(frame, fraction, rng):
+    tx, ty = frame.width // 8, frame.height // 4
+    n = tx * ty
+    k = max(1, int(n * fraction))
+    return np.sort(rng.choice(n, size=k, replace=False))
+
+
+def oracle_sample(view, frames, fraction, nthreads, seed=5, stats=False):
+    """Render a random `fraction` of the 8x4 tiles of every frame on the CPU oracle.
+
+    Returns (rays, seconds, mean node-visit bytes per primary ray incl. its shadow ray)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import ctypes as C
+
+    import oracle as orc
+    import woxel_gb300 as wx
+
+    L = orc.lib()
+    s, keep = orc._view_struct(view)
+    rng = np.random.default_rng(seed)
+    rays, secs, byte_sum = 0, 0.0, 0.0
+    for fr in frames:
+        st = fr.state()
+        sb = C.create_string_buffer(wx.state_bytes(st), 256)
+        tiles = sample_tiles(fr, fraction, rng)
+        rgba = np.zeros((fr.height, fr.width, 4), np.uint8)
+        stt = np.zeros((fr.height, fr.width), orc.STATS_DTYPE) if stats else None
+        tl = np.ascontiguousarray(tiles, np.uint64)
+        t0 = time.perf_counter()
+        rc = L.orc_render_tile_list(C.byref(s), sb, fr.width, fr.height, tl.ctypes.data, tl.size, rgba.ctypes.data,
+                                    None, None if stt is None else stt.ctypes.data, nthreads)
+        secs += time.perf_counter() - t0
+        if rc != 0:
+            raise RuntimeError("oracle tile list out of range")
+        rays += len(tiles) * 32
+        if stats:
+            m = np.zeros((fr.height, fr.width), bool)
+            for t in tiles:
+                x0, y0 = (t % (fr.width // 8)) * 8, (t // (fr.width // 8)) * 4
+                m[y0:y0 + 4, x0:x0 + 8] = True
+            byte_sum += float(stt["bytes"][m].sum() + stt["shadow_bytes"][m].sum())
+    del keep
+    return rays, secs, (byte_sum / rays if stats else None)
+
+
+def run_reference(args, wl_name):
+    """--impl reference: the reference algorithm on the host cores (rank 0 only)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import woxel_gb300 as wx  # noqa: F401
+    from woxel_gb300 import workloads as W
+
+    wl = W.workload(wl_name)
+    topo = wl.grids[wl.frames[0].grid]()
+    view = topo.view()
+    nthreads = os.cpu_count() or 1
+    frac = args.cpu_fraction
+    # warmup: one small sample
+    for _ in range(max(0, min(args.warmup, 1))):
+        oracle_sample(view, wl.frames[:1], frac / 4, nthreads, seed=99)
+    times, rays_tot = [], 0
+    for k in range(args.steps):
+        rays, secs, _ = oracle_sample(view, wl.frames, frac, nthreads, seed=100 + k)
+        times.append(secs)
+        rays_tot += rays
+    total = sum(times)
+    value = rays_tot / total / 1e9
+    line = {
+        "impl": "reference", "metric": "primary_ray_grays_per_s", "value": value, "unit": "Grays/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl_name, "frames": len(wl.frames), "parallelism": "cpu-threads"},
+        "cpu_baseline": {"value": value, "unit": "Grays/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{frac:.4f} of the 8x4 tiles of each of the {len(wl.frames)} frames per step, "
+                                   f"C restatement of raycast.comp.wgsl (oracle/), {nthreads} threads"},
+        "e2e": {"value": value, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "woxel's own pass (Rust + wgpu 0.17 CPU adapter) cannot run here: no Rust toolchain, "
+                "crates not vendored, no graphics stack; timed instead is the oracle's restatement",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="spheres", choices=["sphere", "spheres", "noise"])
+    ap.add_argument("--cpu-fraction", type=float, default=1.0 / 8)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--kernel", default="persistent", choices=["persistent", "pixel"])
+    ap.add_argument("--tile-width", type=int, default=None)
+    ap.add_argument("--warps-per-block", type=int, default=None)
+    ap.add_argument("--blocks-per-sm", type=int, default=None)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args, args.workload)
+        return
+
+    import torch
+
+    import woxel_gb300 as wx
+    from woxel_gb300 import workloads as W
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    wl = W.workload(args.workload)
+    t0 = time.perf_counter()
+    topo = wl.grids[wl.frames[0].grid]()
+    t_gen = time.perf_counter() - t0
+    ctx = wx.Context(local)
+    tune = {"kernel": 0 if args.kernel == "persistent" else 1}
+    for k in ("tile_width", "warps_per_block", "blocks_per_sm"):
+        if getattr(args, k) is not None:
+            tune[k] = getattr(args, k)
+    ctx.set_tuning(**tune)
+    t0 = time.perf_counter()
+    grid = ctx.build_grid(topo)
+    t_build = time.perf_counter() - t0
+    info = grid.info
+    log(f"[bench] grid {args.workload}: {info} gen {t_gen:.1f}s sdf+upload {t_build:.1f}s")
+    frames = wl.frames
+    states = [f.state() for f in frames]
+    W_, H_ = frames[0].width, frames[0].height
+    outs = [torch.empty(W_ * H_ * 4, dtype=torch.uint8, device=dev) for _ in frames]
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+
+    def step(events=None):
+        for i, (st, o) in enumerate(zip(states, outs)):
+            if events is not None:
+                events[i][0].record(stream)
+            ctx.render(grid, st, W_, H_, o, None, stream=sh)
+            if events is not None:
+                events[i][1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+
+    step_ms, launch_ms = [], []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        for _ in range(args.steps):
+            flush.zero_()  # L2 flush between timed iterations (outside the step's events)
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in frames]
+            step(ev)
+            torch.cuda.synchronize()
+            lm = [a.elapsed_time(b) for a, b in ev]
+            launch_ms.extend(lm)
+            step_ms.append(ev[0][0].elapsed_time(ev[-1][1]))
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    ms = statistics.mean(step_ms)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    rays_step = wl.rays
+    value = world * rays_step / (ms / 1e3) / 1e9
+    lat = sorted(launch_ms)
+    p50 = lat[len(lat) // 2]
+    p99 = lat[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]
+
+    # e2e: through wx_render with pinned host output buffers (copies inside the timed region)
+    e2e = None
+    if not args.no_e2e:
+        host = [torch.empty(W_ * H_ * 4, dtype=torch.uint8).pin_memory() for _ in frames]
+
+        def step_host():
+            for st, hb in zip(states, host):
+                ctx.render(grid, st, W_, H_, hb, None, stream=sh)
+
+        step_host()
+        torch.cuda.synchronize()
+        e_ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            step_host()
+            torch.cuda.synchronize()
+            e_ms.append(1e3 * (time.perf_counter() - t1))
+        em = statistics.mean(e_ms)
+        e2e = {"value": world * rays_step / (em / 1e3) / 1e9, "unit": "Grays/s",
+               "h2d_bytes_per_step": 256 * len(frames), "d2h_bytes_per_step": W_ * H_ * 4 * len(frames),
+               "ms_per_step": em}
+
+    # roofline + CPU baseline from the oracle on a sample of the same tiles (rank 0)
+    roof, cpu = None, None
+    if rank == 0:
+        peak, peak_kind = hbm_peak()
+        view = topo.view()
+        nthreads = os.cpu_count() or 1
+        rays_s, secs, bpr = oracle_sample(view, frames, args.cpu_fraction, nthreads, seed=5, stats=True)
+        launch_avg_ms = statistics.mean(launch_ms)
+        bytes_launch = bpr * frames[0].rays
+        achieved = bytes_launch / (launch_avg_ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "peak_kind": peak_kind, "kernel": "k_render_plain",
+                "algorithmic_bytes_per_ray": bpr, "launch_ms": launch_avg_ms}
+        if not args.no_cpu:
+            cpu = {"value": rays_s / secs / 1e9, "unit": "Grays/s", "cores": nthreads, "kind": "port",
+                   "sample": f"{args.cpu_fraction:.4f} of the 8x4 tiles of each of the {len(frames)} frames "
+                             f"({rays_s} rays), C restatement of raycast.comp.wgsl, {nthreads} threads"}
+        del view
+
+    if rank == 0:
+        line = {
+            "metric": "primary_ray_grays_per_s", "value": value, "unit": "Grays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{args.workload}: {len(frames)} x {W_}x{H_} frames, plain per-frame launches",
+                       "grid": {k: info[k] for k in ("n5", "n4", "n3", "active_voxels", "device_bytes")},
+                       "render_mode": frames[0].mode, "l2": "flushed between steps (512 MB write)",
+                       "parallelism": f"replicas x{world}", "tuning": ctx.tuning},
+            "frame_latency_ms": {"p50": p50, "p99": p99},
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+            "gpu_launches": len(frames) * args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -100,6 +100,26 @@ typedef struct wx_grid_info {
 typedef struct wx_ctx wx_ctx;
 typedef struct wx_grid wx_grid;
 typedef struct wx_topology wx_topology;
+typedef struct wx_batch wx_batch;
+
+/* Launch shape of the raycast kernels (set per context; see wx_ctx_set_tuning). */
+typedef struct wx_tuning {
+    int32_t kernel;          /* 0: persistent warps drawing pixel tiles from a queue (default);
+                                1: one warp per tile, tiles in launch order */
+    int32_t warps_per_block; /* 1..8 (default 4) */
+    int32_t blocks_per_sm;   /* persistent kernel: 0 = as many as fit */
+    int32_t tile_width;      /* pixel tile of one warp: 4, 8 (default: the reference's 8x4
+                                workgroup), 16 or 32 wide, 32/tile_width high */
+} wx_tuning;
+
+/* One frame of a batched launch: a camera uniform over one resident grid. */
+typedef struct wx_frame {
+    const wx_grid *grid;
+    wx_state_uniform state;
+    uint32_t width, height;
+    uint8_t *rgba8;  /* device memory, width*height*4 bytes */
+    wx_hit *hits;    /* device memory or NULL */
+} wx_frame;
 
 /* ---- library ---- */
 const char *wx_status_string(int status);
@@ -128,6 +148,30 @@ int wx_grid_get_info(const wx_grid *grid, wx_grid_info *out);
  * cudaStream_t (NULL = legacy default stream). */
 int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, uint32_t width,
               uint32_t height, uint8_t *rgba8, wx_hit *hits, void *stream);
+
+/* ---- launch tuning (no counterpart in the reference: wgpu_context.rs:280
+ * notes the workgroup choice as a TODO) ---- */
+int wx_ctx_set_tuning(wx_ctx *ctx, const wx_tuning *tuning);
+int wx_ctx_get_tuning(const wx_ctx *ctx, wx_tuning *tuning);
+
+/* ---- batched rendering: many cameras over several resident grids in one
+ * persistent launch drawing 8x4 ray tiles from a global queue. Per frame the
+ * result equals wx_render's. No counterpart in the reference, which renders
+ * one frame per dispatch (wgpu_context.rs:270-282). ---- */
+/* One-shot: uploads the frame table and launches on `stream`. */
+int wx_render_batch(wx_ctx *ctx, const wx_frame *frames, uint32_t n, void *stream);
+/* Plan: the frame table is uploaded once and the launch (queue reset +
+ * persistent kernel) is captured in a CUDA graph; wx_batch_launch replays it.
+ * Outputs of the frames are rewritten on every launch. */
+int wx_batch_create(wx_ctx *ctx, const wx_frame *frames, uint32_t n, wx_batch **out);
+int wx_batch_launch(wx_batch *batch, void *stream);
+int wx_batch_info(const wx_batch *batch, uint32_t *frames, uint32_t *tiles, uint64_t *rays);
+int wx_batch_destroy(wx_batch *batch);
+
+/* Exhaustive GPU check of the kernels' fast floor(p / size) path against IEEE
+ * division: every odd divisor m < max_m (<= 4096) and every significand of
+ * [1,2) and [-2,-1). out = {mismatches, first bad m, its x bits}. */
+int wx_check_division(wx_ctx *ctx, uint32_t max_m, uint64_t out[3]);
 
 /* ---- host-side helpers (no GPU needed) ---- */
 /* ComputeState::build (compute_state.rs:87-131) for a look_at_rh camera

@@ -55,6 +55,7 @@ def lib() -> C.CDLL:
                                        C.c_float, P]),
             "orc_render": (I, [P, P, C.c_uint32, C.c_uint32, P, P, P, I]),
             "orc_render_tiles": (I, [P, P, C.c_uint32, C.c_uint32, U64, U64, P, P, P, I]),
+            "orc_render_tile_list": (I, [P, P, C.c_uint32, C.c_uint32, P, U64, P, P, P, I]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -199,6 +200,11 @@ def render(v: dict, state: bytes, width: int, height: int, nthreads: int = 1, hi
     if tiles is None:
         rc = lib().orc_render(C.byref(s), sb, width, height, rgba.ctypes.data,
                               None if h is None else h.ctypes.data, None if st is None else st.ctypes.data, nthreads)
+    elif isinstance(tiles, np.ndarray):
+        tl = np.ascontiguousarray(tiles, np.uint64)
+        rc = lib().orc_render_tile_list(C.byref(s), sb, width, height, tl.ctypes.data, tl.size, rgba.ctypes.data,
+                                        None if h is None else h.ctypes.data,
+                                        None if st is None else st.ctypes.data, nthreads)
     else:
         rc = lib().orc_render_tiles(C.byref(s), sb, width, height, tiles[0], tiles[1], rgba.ctypes.data,
                                     None if h is None else h.ctypes.data, None if st is None else st.ctypes.data,

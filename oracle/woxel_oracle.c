@@ -1031,6 +1031,7 @@ typedef struct {
     const orc_state *s;
     uint32_t width, tiles_x;
     uint64_t tile_begin, tile_end;
+    const uint64_t *list; /* optional: tile indices list[tile_begin..tile_end) */
     uint8_t *rgba;
     orc_hit *hits;
     orc_stats *stats;
@@ -1040,14 +1041,26 @@ typedef struct {
 static void *worker(void *arg) {
     Job *j = (Job *)arg;
     for (;;) {
-        uint64_t tile = atomic_fetch_add(&j->next, 1) + j->tile_begin;
-        if (tile >= j->tile_end) break;
+        uint64_t k = atomic_fetch_add(&j->next, 1) + j->tile_begin;
+        if (k >= j->tile_end) break;
+        uint64_t tile = j->list ? j->list[k] : k;
         uint32_t tx = (uint32_t)(tile % j->tiles_x), ty = (uint32_t)(tile / j->tiles_x);
         for (uint32_t ly = 0; ly < 4; ly++)
             for (uint32_t lx = 0; lx < 8; lx++)
                 shade_pixel(j->v, j->s, tx * 8 + lx, ty * 4 + ly, j->width, j->rgba, j->hits, j->stats);
     }
     return NULL;
+}
+
+static void run_job(Job *j, int nthreads) {
+    if (nthreads <= 1) {
+        worker(j);
+        return;
+    }
+    pthread_t *th = malloc(sizeof(pthread_t) * (size_t)nthreads);
+    for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, worker, j);
+    for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
+    free(th);
 }
 
 int orc_render_tiles(const orc_view *v, const orc_state *s, uint32_t width, uint32_t height,
@@ -1059,17 +1072,25 @@ int orc_render_tiles(const orc_view *v, const orc_state *s, uint32_t width, uint
     if (tile_begin >= tile_end) return 0;
     Job j;
     j.v = v; j.s = s; j.width = width; j.tiles_x = tiles_x;
-    j.tile_begin = tile_begin; j.tile_end = tile_end;
+    j.tile_begin = tile_begin; j.tile_end = tile_end; j.list = NULL;
     j.rgba = rgba; j.hits = hits; j.stats = stats;
     atomic_init(&j.next, 0);
-    if (nthreads <= 1) {
-        worker(&j);
-        return 0;
-    }
-    pthread_t *th = malloc(sizeof(pthread_t) * (size_t)nthreads);
-    for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, worker, &j);
-    for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
-    free(th);
+    run_job(&j, nthreads);
+    return 0;
+}
+
+int orc_render_tile_list(const orc_view *v, const orc_state *s, uint32_t width, uint32_t height,
+                         const uint64_t *tiles, uint64_t ntiles, uint8_t *rgba, orc_hit *hits,
+                         orc_stats *stats, int nthreads) {
+    uint64_t total = (uint64_t)(width / 8) * (height / 4);
+    for (uint64_t i = 0; i < ntiles; i++)
+        if (tiles[i] >= total) return 1;
+    Job j;
+    j.v = v; j.s = s; j.width = width; j.tiles_x = width / 8;
+    j.tile_begin = 0; j.tile_end = ntiles; j.list = tiles;
+    j.rgba = rgba; j.hits = hits; j.stats = stats;
+    atomic_init(&j.next, 0);
+    run_job(&j, nthreads);
     return 0;
 }
 

@@ -129,6 +129,10 @@ int orc_render(const orc_view *v, const orc_state *s, uint32_t width, uint32_t h
 int orc_render_tiles(const orc_view *v, const orc_state *s, uint32_t width, uint32_t height,
                      uint64_t tile_begin, uint64_t tile_end, uint8_t *rgba, orc_hit *hits,
                      orc_stats *stats, int nthreads);
+/* Same, for an explicit list of tile indices (row-major over the 8x4 tile grid). */
+int orc_render_tile_list(const orc_view *v, const orc_state *s, uint32_t width, uint32_t height,
+                         const uint64_t *tiles, uint64_t ntiles, uint8_t *rgba, orc_hit *hits,
+                         orc_stats *stats, int nthreads);
 
 #ifdef __cplusplus
 }

@@ -8,6 +8,24 @@ from parity import compare, dispatch_mask, gpu_render, oracle_render
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=["persistent", "pixel", "pixel-16x2", "persistent-4x8"], autouse=True)
+def kernel(request, cuda_ctx):
+    """Run every parity test on both kernels and on non-default pixel tile shapes."""
+    before = cuda_ctx.tuning
+    tw = {"pixel-16x2": 16, "persistent-4x8": 4}.get(request.param, 8)
+    cuda_ctx.set_tuning(kernel=0 if request.param.startswith("persistent") else 1, tile_width=tw)
+    yield request.param
+    cuda_ctx.set_tuning(**before)
+
+
+def test_fast_division_matches_ieee(cuda_ctx, kernel):
+    """Every odd divisor m < 4096 and every significand of [1,2) and [-2,-1): bit-equal to IEEE x/m."""
+    if kernel != "persistent":
+        pytest.skip("kernel independent")
+    bad, m, xbits = cuda_ctx.check_division(4096)
+    assert bad == 0, f"{bad} mismatches, first m={m} x=0x{xbits:08x}"
+
+
 @pytest.fixture(scope="module")
 def sphere64(cuda_ctx):
     topo = wx.Topology.sphere((0, 0, 0), 64.0, 3.0)

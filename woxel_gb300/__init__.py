@@ -15,8 +15,8 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-from ._ffi import (WX_OK, WxError, check, lib, wx_grid_info, wx_hit, wx_state_uniform,  # noqa: F401
-                   wx_vdb345_view)
+from ._ffi import (WX_OK, WxError, check, lib, wx_frame, wx_grid_info, wx_hit, wx_state_uniform,  # noqa: F401
+                   wx_tuning, wx_vdb345_view)
 
 HIT_DTYPE = np.dtype([("p", "<f4", (3,)), ("t", "<f4"), ("node", "<u4"), ("info", "<u4"),
                       ("shadow", "<u4"), ("reserved", "<u4")])
@@ -253,3 +253,71 @@ class Context:
         """One frame: rgba (w*h*4 bytes) and hits (w*h records) are device tensors or host arrays."""
         check(lib().wx_render(self._h, grid._h, C.byref(state), width, height, _ptr(rgba), _ptr(hits),
                               None if stream is None else int(stream)), self._h)
+
+    @property
+    def tuning(self) -> dict:
+        t = wx_tuning()
+        check(lib().wx_ctx_get_tuning(self._h, C.byref(t)), self._h)
+        return {k: int(getattr(t, k)) for k, _ in wx_tuning._fields_}
+
+    def set_tuning(self, **kw) -> None:
+        cur = self.tuning
+        cur.update(kw)
+        t = wx_tuning(**cur)
+        check(lib().wx_ctx_set_tuning(self._h, C.byref(t)), self._h)
+
+    def check_division(self, max_m: int = 4096) -> tuple:
+        out = (C.c_uint64 * 3)()
+        check(lib().wx_check_division(self._h, max_m, out), self._h)
+        return int(out[0]), int(out[1]), int(out[2])
+
+    @staticmethod
+    def _frames(frames: Sequence) -> "C.Array":
+        arr = (wx_frame * len(frames))()
+        for i, (grid, state, w, h, rgba, hits) in enumerate(frames):
+            arr[i].grid = grid._h.value
+            arr[i].state = state
+            arr[i].width, arr[i].height = w, h
+            arr[i].rgba8 = _ptr(rgba)
+            arr[i].hits = _ptr(hits)
+        return arr
+
+    def render_batch(self, frames: Sequence, stream=None) -> None:
+        """frames: (grid, state, width, height, rgba_dev, hits_dev_or_None) tuples; one persistent launch."""
+        arr = self._frames(frames)
+        check(lib().wx_render_batch(self._h, arr, len(frames), None if stream is None else int(stream)), self._h)
+
+    def batch(self, frames: Sequence) -> "Batch":
+        arr = self._frames(frames)
+        out = C.c_void_p()
+        check(lib().wx_batch_create(self._h, arr, len(frames), C.byref(out)), self._h)
+        return Batch(self, out.value, [f[0] for f in frames])
+
+
+class Batch:
+    """A batched launch captured in a CUDA graph (wx_batch_create / wx_batch_launch)."""
+
+    def __init__(self, ctx: Context, handle: int, grids: list):
+        self.ctx = ctx
+        self._h = C.c_void_p(handle)
+        self._grids = grids  # keep the grids alive while the plan exists
+
+    def launch(self, stream=None) -> None:
+        check(lib().wx_batch_launch(self._h, None if stream is None else int(stream)), self.ctx._h)
+
+    @property
+    def info(self) -> dict:
+        f, t, r = C.c_uint32(), C.c_uint32(), C.c_uint64()
+        check(lib().wx_batch_info(self._h, C.byref(f), C.byref(t), C.byref(r)))
+        return {"frames": f.value, "tiles": t.value, "rays": r.value}
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            lib().wx_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

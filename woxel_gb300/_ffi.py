@@ -35,6 +35,16 @@ class wx_grid_info(C.Structure):
                 ("active_voxels", C.c_uint64)]
 
 
+class wx_tuning(C.Structure):
+    _fields_ = [("kernel", C.c_int32), ("warps_per_block", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("tile_width", C.c_int32)]
+
+
+class wx_frame(C.Structure):
+    _fields_ = [("grid", C.c_void_p), ("state", wx_state_uniform), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("rgba8", C.c_void_p), ("hits", C.c_void_p)]
+
+
 assert C.sizeof(wx_state_uniform) == 256
 assert C.sizeof(wx_hit) == 32
 
@@ -54,6 +64,14 @@ SIGNATURES = {
     "wx_grid_release": (INT, [P, P]),
     "wx_grid_get_info": (INT, [P, C.POINTER(wx_grid_info)]),
     "wx_render": (INT, [P, P, C.POINTER(wx_state_uniform), U32, U32, P, P, P]),
+    "wx_ctx_set_tuning": (INT, [P, C.POINTER(wx_tuning)]),
+    "wx_ctx_get_tuning": (INT, [P, C.POINTER(wx_tuning)]),
+    "wx_render_batch": (INT, [P, C.POINTER(wx_frame), U32, P]),
+    "wx_batch_create": (INT, [P, C.POINTER(wx_frame), U32, C.POINTER(P)]),
+    "wx_batch_launch": (INT, [P, P]),
+    "wx_batch_info": (INT, [P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U64)]),
+    "wx_batch_destroy": (INT, [P]),
+    "wx_check_division": (INT, [P, U32, C.POINTER(U64)]),
     "wx_state_build": (INT, [P, P, P, F32, F32, F32, U32, P, P, P, F32, C.POINTER(wx_state_uniform)]),
     "wx_sun_default": (None, [P, P, P]),
     "wx_topology_from_masks": (INT, [P, P, U64, P, P, U64, P, U64, P, U32, C.POINTER(P)]),

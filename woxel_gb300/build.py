@@ -24,8 +24,9 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true",
               "-ftz=false", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread"]
 
-CU_SOURCES = ["render.cu"]
-CXX_SOURCES = ["topology.cpp", "scene.cpp"]
+CU_SOURCES = ["kernels.cu"]
+CXX_SOURCES = ["api.cpp", "topology.cpp", "scene.cpp"]
+CUDA_INC = ["-I", "/usr/local/cuda/include"]
 
 
 def _nvcc() -> str:
@@ -63,7 +64,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         obj = BUILD / (Path(src).stem + ".o")
         objs.append(obj)
         if force or _stale(obj, [CSRC / src, *headers]):
-            jobs.append(["g++", *CXX_FLAGS, *inc, "-c", str(CSRC / src), "-o", str(obj)])
+            jobs.append(["g++", *CXX_FLAGS, *inc, *CUDA_INC, "-c", str(CSRC / src), "-o", str(obj)])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         outs = list(ex.map(_run, jobs))
     if verbose:

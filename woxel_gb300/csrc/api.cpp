@@ -1,7 +1,7 @@
-// render.cu — device node pools, the plain per-frame raycast kernel and the
-// C ABI around them (context, grid upload/build, render).
+// api.cpp — the C ABI (include/woxel_gb300.h): contexts, grid upload/build,
+// per-frame render, batched render (one-shot and CUDA-graph plans), tuning.
 //
-// Device layout (uploaded once per grid, immutable afterwards):
+// Device layout of a grid (uploaded once, immutable afterwards):
 //   o5     n5 x int4         N5 origins (root keys) in DFS order
 //   slot5  n5 x 32768 u32    per N4-sized slot: child flag|N4 index, or skip distance
 //   slot4  n4 x  4096 u32    per N3-sized slot: child flag|N3 index, or skip distance
@@ -16,28 +16,55 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <new>
 #include <string>
 #include <thread>
 #include <vector>
 
 #include "wx_common.h"
-#include "wx_device.cuh"
+#include "wx_kernels.h"
+
+namespace {
+constexpr uint32_t kCounterSlots = 1u << 16;  // one work counter per in-flight launch (ring)
+}
 
 struct wx_ctx {
     int device = 0;
+    int num_sms = 0;
     std::string err;
-    void *stage = nullptr;  // device staging for host-memory outputs
+    wxk::Tuning tuning;
+    uint32_t *counters = nullptr;       // kCounterSlots device counters
+    uint32_t next_counter = 0;
+    unsigned long long *check = nullptr;  // division self-check results
+    void *stage = nullptr;              // device staging for host-memory outputs
     size_t stage_bytes = 0;
+    wxk::Job *jobs_dev = nullptr;       // job table of the one-shot batch entry point
+    size_t jobs_cap = 0;
+    wxk::Job *jobs_host = nullptr;      // pinned staging for that table
+    cudaEvent_t jobs_done = nullptr;    // last one-shot batch's table copy
+    uint32_t *take_counter() {
+        uint32_t *c = counters + next_counter;
+        next_counter = (next_counter + 1) % kCounterSlots;
+        return c;
+    }
 };
 
 struct wx_grid {
     int device = 0;
     void *dev = nullptr;
     size_t bytes = 0;
-    wxd::DevGrid g{};
+    wxk::DevGrid g{};
     wx_grid_info info{};
+};
+
+struct wx_batch {
+    wx_ctx *ctx = nullptr;
+    wxk::Job *jobs_dev = nullptr;
+    uint32_t njobs = 0, total_tiles = 0;
+    uint64_t rays = 0;
+    uint32_t *counter = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
 };
 
 namespace {
@@ -51,35 +78,11 @@ int cuda_fail(wx_ctx *ctx, cudaError_t e, const char *what) {
     return fail(ctx, e == cudaErrorMemoryAllocation ? WX_ERR_OOM : WX_ERR_CUDA,
                 std::string(what) + ": " + cudaGetErrorString(e));
 }
-#define WX_CUDA(ctx, call)                                   \
-    do {                                                     \
-        cudaError_t e_ = (call);                             \
+#define WX_CUDA(ctx, call)                                       \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
         if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
     } while (0)
-
-constexpr int kWarpsPerBlock = 4;
-
-__global__ void __launch_bounds__(32 * kWarpsPerBlock)
-    k_render_plain(wxd::DevGrid g, wx_state_uniform s, uint32_t width, uint32_t tiles_x, uint32_t ntiles,
-                   uint32_t *__restrict__ rgba, wx_hit *__restrict__ hits) {
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t tile = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-    if (tile >= ntiles) return;
-    // One warp = one 8x4 pixel tile, the reference's workgroup (raycast.comp.wgsl:60).
-    const uint32_t gx = (tile % tiles_x) * 8u + (lane & 7u);
-    const uint32_t gy = (tile / tiles_x) * 4u + (lane >> 3);
-    uint32_t c;
-    wx_hit rec;
-    wxd::shade_pixel(g, s, gx, gy, c, rec);
-    const size_t pix = (size_t)gy * width + gx;
-    rgba[pix] = c;
-    if (hits) {
-        uint4 *h = reinterpret_cast<uint4 *>(hits + pix);
-        h[0] = make_uint4(__float_as_uint(rec.p[0]), __float_as_uint(rec.p[1]), __float_as_uint(rec.p[2]),
-                          __float_as_uint(rec.t));
-        h[1] = make_uint4(rec.node, rec.info, rec.shadow, 0u);
-    }
-}
 
 bool device_accessible(const void *p) {
     cudaPointerAttributes a;
@@ -134,6 +137,27 @@ void parallel_chunks(size_t n, F f) {
     for (auto &x : th) x.join();
 }
 
+// Tiles of tile_w x (32 / tile_w) pixels over the dispatched region
+// 8*floor(w/8) x 4*floor(h/4) (wgpu_context.rs:281).
+wxk::Job make_job(const wx_grid *grid, const wx_state_uniform &s, uint32_t width, uint32_t height, uint32_t *rgba,
+                  wx_hit *hits, uint32_t tile_begin, int tile_w) {
+    wxk::Job j;
+    memset(&j, 0, sizeof j);
+    j.g = grid->g;
+    j.width = width;
+    j.height = height;
+    j.tile_w = (uint32_t)tile_w;
+    j.tile_h = 32u / j.tile_w;
+    const uint32_t wd = width & ~7u, hd = height & ~3u;
+    j.tiles_x = (wd + j.tile_w - 1) / j.tile_w;
+    j.tiles = j.tiles_x * ((hd + j.tile_h - 1) / j.tile_h);
+    j.tile_begin = tile_begin;
+    j.rgba = rgba;
+    j.hits = hits;
+    j.s = s;
+    return j;
+}
+
 }  // namespace
 
 extern "C" {
@@ -159,10 +183,24 @@ int wx_ctx_create(int device, wx_ctx **out) {
     if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDeviceCount");
     if (device < 0 || device >= n) return fail(nullptr, WX_ERR_INVALID, "wx_ctx_create: no such device");
     WX_CUDA(nullptr, cudaSetDevice(device));
-    WX_CUDA(nullptr, cudaFree(nullptr));
     auto *c = new (std::nothrow) wx_ctx();
     if (!c) return fail(nullptr, WX_ERR_OOM, "host allocation failed");
     c->device = device;
+    auto cleanup = [&](cudaError_t err, const char *what) {
+        wx_ctx_destroy(c);
+        return cuda_fail(nullptr, err, what);
+    };
+    if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
+        return cleanup(e, "cudaDeviceGetAttribute");
+    if ((e = wxk::init_device_tables()) != cudaSuccess) return cleanup(e, "init_device_tables");
+    if ((e = cudaMalloc(&c->counters, kCounterSlots * sizeof(uint32_t))) != cudaSuccess)
+        return cleanup(e, "cudaMalloc(counters)");
+    if ((e = cudaMemset(c->counters, 0, kCounterSlots * sizeof(uint32_t))) != cudaSuccess)
+        return cleanup(e, "cudaMemset(counters)");
+    if ((e = cudaMalloc(&c->check, 4 * sizeof(unsigned long long))) != cudaSuccess)
+        return cleanup(e, "cudaMalloc(check)");
+    if ((e = cudaEventCreateWithFlags(&c->jobs_done, cudaEventDisableTiming)) != cudaSuccess)
+        return cleanup(e, "cudaEventCreate");
     *out = c;
     return WX_OK;
 }
@@ -170,12 +208,52 @@ int wx_ctx_create(int device, wx_ctx **out) {
 int wx_ctx_destroy(wx_ctx *ctx) {
     if (!ctx) return WX_OK;
     cudaSetDevice(ctx->device);
+    if (ctx->jobs_done) {
+        cudaEventSynchronize(ctx->jobs_done);
+        cudaEventDestroy(ctx->jobs_done);
+    }
     if (ctx->stage) cudaFree(ctx->stage);
+    if (ctx->counters) cudaFree(ctx->counters);
+    if (ctx->check) cudaFree(ctx->check);
+    if (ctx->jobs_dev) cudaFree(ctx->jobs_dev);
+    if (ctx->jobs_host) cudaFreeHost(ctx->jobs_host);
     delete ctx;
     return WX_OK;
 }
 
 const char *wx_last_error(const wx_ctx *ctx) { return ctx ? ctx->err.c_str() : wx_thread_last_error(); }
+
+int wx_ctx_set_tuning(wx_ctx *ctx, const wx_tuning *t) {
+    if (!ctx || !t) return fail(ctx, WX_ERR_INVALID, "wx_ctx_set_tuning: null argument");
+    const bool tw_ok = t->tile_width == 4 || t->tile_width == 8 || t->tile_width == 16 || t->tile_width == 32;
+    if (t->kernel < 0 || t->kernel > 1 || t->warps_per_block < 1 || t->warps_per_block > 8 || t->blocks_per_sm < 0 ||
+        t->blocks_per_sm > 64 || !tw_ok)
+        return fail(ctx, WX_ERR_INVALID, "wx_ctx_set_tuning: value out of range");
+    ctx->tuning.kernel = t->kernel;
+    ctx->tuning.warps_per_block = t->warps_per_block;
+    ctx->tuning.blocks_per_sm = t->blocks_per_sm;
+    ctx->tuning.tile_w = t->tile_width;
+    return WX_OK;
+}
+
+int wx_ctx_get_tuning(const wx_ctx *ctx, wx_tuning *t) {
+    if (!ctx || !t) return WX_ERR_INVALID;
+    t->kernel = ctx->tuning.kernel;
+    t->warps_per_block = ctx->tuning.warps_per_block;
+    t->blocks_per_sm = ctx->tuning.blocks_per_sm;
+    t->tile_width = ctx->tuning.tile_w;
+    return WX_OK;
+}
+
+int wx_check_division(wx_ctx *ctx, uint32_t max_m, uint64_t out[3]) {
+    if (!ctx || !out) return fail(ctx, WX_ERR_INVALID, "wx_check_division: null argument");
+    WX_CUDA(ctx, cudaSetDevice(ctx->device));
+    WX_CUDA(ctx, wxk::check_division(max_m, ctx->check, nullptr));
+    unsigned long long h[3];
+    WX_CUDA(ctx, cudaMemcpy(h, ctx->check, sizeof h, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 3; i++) out[i] = h[i];
+    return WX_OK;
+}
 
 int wx_grid_build(wx_ctx *ctx, wx_topology *t, wx_grid **out) {
     if (!ctx || !t || !out) return fail(ctx, WX_ERR_INVALID, "wx_grid_build: null argument");
@@ -362,15 +440,17 @@ int wx_grid_get_info(const wx_grid *grid, wx_grid_info *out) {
     return WX_OK;
 }
 
-int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, uint32_t width,
-              uint32_t height, uint8_t *rgba8, wx_hit *hits, void *stream) {
+int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, uint32_t width, uint32_t height,
+              uint8_t *rgba8, wx_hit *hits, void *stream) {
     if (!ctx || !grid || !state || !rgba8) return fail(ctx, WX_ERR_INVALID, "wx_render: null argument");
     if (grid->device != ctx->device) return fail(ctx, WX_ERR_INVALID, "wx_render: grid is on another device");
+    if (((uintptr_t)rgba8 & 3) || ((uintptr_t)hits & 15))
+        return fail(ctx, WX_ERR_INVALID, "wx_render: rgba8 must be 4-byte and hits 16-byte aligned");
     WX_CUDA(ctx, cudaSetDevice(ctx->device));
     const uint32_t tiles_x = width / 8, tiles_y = height / 4;
     const uint64_t ntiles = (uint64_t)tiles_x * tiles_y;
     if (ntiles == 0) return WX_OK;
-    if (ntiles > (1ull << 31)) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_render: frame too large");
+    if ((uint64_t)width * height >= (1ull << 32)) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_render: frame too large");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const bool dev_rgba = device_accessible(rgba8);
     const bool dev_hits = hits ? device_accessible(hits) : true;
@@ -380,7 +460,10 @@ int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, u
     if (!dev_rgba || !dev_hits) {
         const size_t need = npix * 4 + (hits ? npix * sizeof(wx_hit) + 256 : 0);
         if (need > ctx->stage_bytes) {
-            if (ctx->stage) cudaFree(ctx->stage);
+            if (ctx->stage) {
+                WX_CUDA(ctx, cudaStreamSynchronize(st));
+                cudaFree(ctx->stage);
+            }
             ctx->stage = nullptr;
             ctx->stage_bytes = 0;
             WX_CUDA(ctx, cudaMalloc(&ctx->stage, need));
@@ -390,10 +473,9 @@ int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, u
         if (!dev_rgba) out_rgba = reinterpret_cast<uint32_t *>(b);
         if (hits && !dev_hits) out_hits = reinterpret_cast<wx_hit *>(b + ((npix * 4 + 255) & ~(size_t)255));
     }
-    const uint32_t blocks = (uint32_t)((ntiles + kWarpsPerBlock - 1) / kWarpsPerBlock);
-    k_render_plain<<<blocks, 32 * kWarpsPerBlock, 0, st>>>(grid->g, *state, width, tiles_x, (uint32_t)ntiles,
-                                                         out_rgba, out_hits);
-    WX_CUDA(ctx, cudaGetLastError());
+    const wxk::Job job = make_job(grid, *state, width, height, out_rgba, out_hits, 0, ctx->tuning.tile_w);
+    if (ctx->tuning.kernel == 1) WX_CUDA(ctx, wxk::launch_pixel(job, ctx->tuning, st));
+    else WX_CUDA(ctx, wxk::launch_persistent(job, ctx->take_counter(), ctx->tuning, ctx->num_sms, st));
     // Copy back only the dispatched region; the rest of a host buffer is untouched.
     if (!dev_rgba)
         WX_CUDA(ctx, cudaMemcpy2DAsync(rgba8, (size_t)width * 4, out_rgba, (size_t)width * 4, (size_t)tiles_x * 32,
@@ -402,6 +484,138 @@ int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, u
         WX_CUDA(ctx, cudaMemcpy2DAsync(hits, (size_t)width * sizeof(wx_hit), out_hits, (size_t)width * sizeof(wx_hit),
                                        (size_t)tiles_x * 8 * sizeof(wx_hit), (size_t)tiles_y * 4,
                                        cudaMemcpyDeviceToHost, st));
+    return WX_OK;
+}
+
+// ---- batched rendering: many frames of several grids in one persistent launch ----
+static int build_jobs(wx_ctx *ctx, const wx_frame *frames, uint32_t n, std::vector<wxk::Job> &jobs,
+                      uint32_t *total_tiles, uint64_t *rays) {
+    jobs.clear();
+    uint64_t tiles = 0, r = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const wx_frame &f = frames[i];
+        if (!f.grid || !f.rgba8) return fail(ctx, WX_ERR_INVALID, "wx_frame: null grid or rgba8");
+        if (((uintptr_t)f.rgba8 & 3) || ((uintptr_t)f.hits & 15))
+            return fail(ctx, WX_ERR_INVALID, "wx_frame: rgba8 must be 4-byte and hits 16-byte aligned");
+        if (f.grid->device != ctx->device) return fail(ctx, WX_ERR_INVALID, "wx_frame: grid is on another device");
+        if (!device_accessible(f.rgba8) || (f.hits && !device_accessible(f.hits)))
+            return fail(ctx, WX_ERR_INVALID, "wx_frame: batched outputs must be device memory");
+        if ((uint64_t)f.width * f.height >= (1ull << 32)) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_frame: too large");
+        const wxk::Job j = make_job(f.grid, f.state, f.width, f.height, reinterpret_cast<uint32_t *>(f.rgba8), f.hits,
+                                    (uint32_t)tiles, ctx->tuning.tile_w);
+        if (j.tiles == 0) continue;
+        jobs.push_back(j);
+        tiles += j.tiles;
+        r += (uint64_t)(f.width & ~7u) * (f.height & ~3u);
+        if (tiles >= (1ull << 31)) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_render_batch: more than 2^31 tiles");
+    }
+    *total_tiles = (uint32_t)tiles;
+    *rays = r;
+    return WX_OK;
+}
+
+int wx_render_batch(wx_ctx *ctx, const wx_frame *frames, uint32_t n, void *stream) {
+    if (!ctx || (n && !frames)) return fail(ctx, WX_ERR_INVALID, "wx_render_batch: null argument");
+    WX_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<wxk::Job> jobs;
+    uint32_t total = 0;
+    uint64_t rays = 0;
+    int rc = build_jobs(ctx, frames, n, jobs, &total, &rays);
+    if (rc != WX_OK) return rc;
+    if (jobs.empty()) return WX_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // The pinned staging table is reused: wait for the previous batch's copy.
+    WX_CUDA(ctx, cudaEventSynchronize(ctx->jobs_done));
+    if (jobs.size() > ctx->jobs_cap) {
+        if (ctx->jobs_dev) {
+            WX_CUDA(ctx, cudaDeviceSynchronize());
+            cudaFree(ctx->jobs_dev);
+            cudaFreeHost(ctx->jobs_host);
+        }
+        ctx->jobs_dev = nullptr;
+        ctx->jobs_host = nullptr;
+        ctx->jobs_cap = 0;
+        const size_t cap = std::max<size_t>(jobs.size(), 256);
+        WX_CUDA(ctx, cudaMalloc(&ctx->jobs_dev, cap * sizeof(wxk::Job)));
+        WX_CUDA(ctx, cudaMallocHost(&ctx->jobs_host, cap * sizeof(wxk::Job)));
+        ctx->jobs_cap = cap;
+    }
+    memcpy(ctx->jobs_host, jobs.data(), jobs.size() * sizeof(wxk::Job));
+    WX_CUDA(ctx, cudaMemcpyAsync(ctx->jobs_dev, ctx->jobs_host, jobs.size() * sizeof(wxk::Job),
+                                 cudaMemcpyHostToDevice, st));
+    WX_CUDA(ctx, cudaEventRecord(ctx->jobs_done, st));
+    WX_CUDA(ctx, wxk::launch_batched(ctx->jobs_dev, (uint32_t)jobs.size(), total, ctx->take_counter(), ctx->tuning,
+                                     ctx->num_sms, st));
+    return WX_OK;
+}
+
+int wx_batch_create(wx_ctx *ctx, const wx_frame *frames, uint32_t n, wx_batch **out) {
+    if (!ctx || !out || (n && !frames)) return fail(ctx, WX_ERR_INVALID, "wx_batch_create: null argument");
+    WX_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<wxk::Job> jobs;
+    uint32_t total = 0;
+    uint64_t rays = 0;
+    int rc = build_jobs(ctx, frames, n, jobs, &total, &rays);
+    if (rc != WX_OK) return rc;
+    auto *b = new (std::nothrow) wx_batch();
+    if (!b) return fail(ctx, WX_ERR_OOM, "host allocation failed");
+    b->ctx = ctx;
+    b->njobs = (uint32_t)jobs.size();
+    b->total_tiles = total;
+    b->rays = rays;
+    auto bail = [&](cudaError_t e, const char *what) {
+        wx_batch_destroy(b);
+        return cuda_fail(ctx, e, what);
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&b->jobs_dev, std::max<size_t>(jobs.size(), 1) * sizeof(wxk::Job))) != cudaSuccess)
+        return bail(e, "cudaMalloc(job table)");
+    if (!jobs.empty() &&
+        (e = cudaMemcpy(b->jobs_dev, jobs.data(), jobs.size() * sizeof(wxk::Job), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return bail(e, "cudaMemcpy(job table)");
+    if ((e = cudaMalloc(&b->counter, sizeof(uint32_t))) != cudaSuccess) return bail(e, "cudaMalloc(counter)");
+    // Capture counter reset + persistent launch into a graph, replayed by wx_batch_launch.
+    cudaStream_t cs;
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
+    if ((e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+        cudaStreamDestroy(cs);
+        return bail(e, "cudaStreamBeginCapture");
+    }
+    cudaError_t le = b->njobs ? wxk::launch_batched(b->jobs_dev, b->njobs, total, b->counter, ctx->tuning,
+                                                    ctx->num_sms, cs)
+                              : cudaMemsetAsync(b->counter, 0, sizeof(uint32_t), cs);
+    e = cudaStreamEndCapture(cs, &b->graph);
+    cudaStreamDestroy(cs);
+    if (le != cudaSuccess) return bail(le, "capture launch_batched");
+    if (e != cudaSuccess) return bail(e, "cudaStreamEndCapture");
+    if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess) return bail(e, "cudaGraphInstantiate");
+    *out = b;
+    return WX_OK;
+}
+
+int wx_batch_launch(wx_batch *b, void *stream) {
+    if (!b) return WX_ERR_INVALID;
+    WX_CUDA(b->ctx, cudaSetDevice(b->ctx->device));
+    WX_CUDA(b->ctx, cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream)));
+    return WX_OK;
+}
+
+int wx_batch_info(const wx_batch *b, uint32_t *frames, uint32_t *tiles, uint64_t *rays) {
+    if (!b) return WX_ERR_INVALID;
+    if (frames) *frames = b->njobs;
+    if (tiles) *tiles = b->total_tiles;
+    if (rays) *rays = b->rays;
+    return WX_OK;
+}
+
+int wx_batch_destroy(wx_batch *b) {
+    if (!b) return WX_OK;
+    cudaSetDevice(b->ctx->device);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->jobs_dev) cudaFree(b->jobs_dev);
+    if (b->counter) cudaFree(b->counter);
+    delete b;
     return WX_OK;
 }
 

@@ -1,10 +1,10 @@
 // wx_device.cuh — device-side HDDA march and shading for sm_103a.
 //
 // Restates src/shaders/raycast.comp.wgsl:60-519 over the device node pools
-// (one u32 slot word per child slot; see wx_common.h). Every FP32 operation
-// keeps the shader's order; the translation unit is compiled with
-// -fmad=false (no contraction) and IEEE division/square root, so each ray
-// performs the same operation sequence as the CPU restatement and the
+// (one u32 slot word per child slot; see wx_common.h). Every FP32 operation of
+// the shader keeps its order; the translation unit is compiled with
+// -fmad=false (no contraction), and division / square root are IEEE, so each
+// ray performs the same operation sequence as the CPU restatement and the
 // results are bit-identical. Choices WGSL leaves open are pinned:
 // normalize(v) = v / sqrt((x*x + y*y) + z*z); min/max return the non-NaN
 // operand and the first operand on ties; f32->i32 saturates (NaN -> 0);
@@ -14,27 +14,53 @@
 #include <cstdint>
 
 #include "woxel_gb300.h"
+#include "wx_kernels.h"
 
 namespace wxd {
 
 constexpr uint32_t kChild = 0x80000000u;
 constexpr uint32_t kMaxSteps = 1000u;  // HDDA_MAX_RAY_STEPS, raycast.comp.wgsl:82
 
-struct DevGrid {
-    const int4 *o5;         // N5 origins (x, y, z, 0), DFS order
-    const uint32_t *slot5;  // n5 * 32768
-    const uint32_t *slot4;  // n4 * 4096
-    const uint32_t *slot3;  // n3 * 512
-    uint32_t n5;
-};
+// o5: N5 origins (x, y, z, 0) in DFS order; slot5/4/3: n5*32768, n4*4096, n3*512 slot words.
+using DevGrid = wxk::DevGrid;
 
-struct Uniform {  // the 256-byte ComputeState, read from kernel parameter space
-    wx_state_uniform s;
-};
+// RN(1 / (2j + 1)) for j < kRcpOdd: filled once per device from host IEEE
+// division (wxk::init_device_tables). Defined here: kernels.cu is the only
+// translation unit that includes this header.
+constexpr uint32_t kRcpOdd = 2048;
+__device__ float g_rcp_odd[kRcpOdd];
 
 __device__ __forceinline__ float pmin(float a, float b) { return (b < a || a != a) ? b : a; }
 __device__ __forceinline__ float pmax(float a, float b) { return (b > a || a != a) ? b : a; }
 __device__ __forceinline__ float sign11(float x) { return x < 0.0f ? -1.0f : 1.0f; }
+
+// RN(p / size) for the three coordinates of one step. size = dist * 2^sk =
+// m * 2^k with m odd, so y = RN(1/m) * 2^-k equals RN(1/size) exactly (a
+// power-of-two scaling). With q0 = RN(p*y), the residual e = p - q0*size is
+// exact in one FMA and RN(q0 + e*y) is the correctly rounded quotient
+// (Markstein, IBM J. Res. Dev. 34(1), 1990). The identity is invariant under
+// power-of-two scaling while every intermediate stays a normal number, so the
+// exhaustive GPU check over every odd m < 4096 and every significand of
+// [1,2) and [-2,-1) (wx_check_division) covers every exponent. The result is
+// bit-identical to __fdiv_rn except that a zero quotient may come out +0 for
+// p = -0; the march cannot observe that sign (mod = p - size*floor(q) enters
+// only size*step01 - mod, where +0 and -0 give the same value). Other cases
+// (m >= 4096, or 0 < |p| < 2^-64 where q0 could underflow) take __fdiv_rn.
+__device__ __forceinline__ float rcp_size(uint32_t dist, int sk, bool *fast) {
+    const int tz = __ffs((int)dist) - 1;  // dist >= 1, so k = tz + sk <= 43
+    const uint32_t m = dist >> tz;
+    *fast = m < 2u * kRcpOdd;
+    const float r = __ldg(&g_rcp_odd[(*fast ? m : 1u) >> 1]);
+    return r * __int_as_float((127 - tz - sk) << 23);
+}
+__device__ __forceinline__ bool tiny_nonzero(float p) {  // 0 < |p| < 2^-64
+    return (__float_as_uint(p) & 0x7FFFFFFFu) - 1u < 0x1F7FFFFFu;
+}
+__device__ __forceinline__ float div_fast(float p, float size, float y) {
+    const float q0 = p * y;
+    const float e = __fmaf_rn(-q0, size, p);
+    return __fmaf_rn(e, y, q0);
+}
 
 struct F3 {
     float x, y, z;
@@ -64,6 +90,133 @@ __device__ __forceinline__ uint32_t unorm8(float x) {
     return (uint32_t)floorf(y + 0.5f);
 }
 
+// State of one hdda_ray (raycast.comp.wgsl:84-126) between iterations. The
+// cached parent chain of get_vdb_leaf_from_leaf (:360-396) is kept as the
+// pool indices of the cached N5/N4/N3 plus the voxel of the previous lookup:
+// that voxel lies inside every cached node (levels 1..np), so "pos is in the
+// cached node of side S" is ((x ^ lx) | (y ^ ly) | (z ^ lz)) & ~(S - 1) == 0.
+// Per-ray constants: idir = 1/dir, and n = 4e-4 * sign11(dir), the nudge of
+// :122 (step01 = max(0, sign11(dir)) is n > 0).
+struct Ray {
+    float px, py, pz;
+    float dx, dy, dz;
+    float ix, iy, iz;
+    float nx, ny, nz;
+    int lx, ly, lz;
+    uint32_t np, i5, i4, i3;
+    uint32_t mask, i;
+};
+
+__device__ __forceinline__ void ray_init(Ray &r, F3 src, F3 dir) {
+    r.px = src.x; r.py = src.y; r.pz = src.z;
+    r.dx = dir.x; r.dy = dir.y; r.dz = dir.z;
+    r.ix = __frcp_rn(dir.x); r.iy = __frcp_rn(dir.y); r.iz = __frcp_rn(dir.z);
+    r.nx = 4e-4f * sign11(dir.x); r.ny = 4e-4f * sign11(dir.y); r.nz = 4e-4f * sign11(dir.z);
+    r.lx = r.ly = r.lz = 0;
+    r.np = 0; r.i5 = r.i4 = r.i3 = 0;
+    r.mask = 0;
+    r.i = 0;
+}
+
+// One loop iteration of hdda_ray. Returns 0xFF while the march continues,
+// otherwise the final state (0 hit, 1 out of bounds, 2 step cap); on return
+// r.i is the iteration count the shader reports.
+__device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
+    if (r.i >= kMaxSteps) return 2u;
+    // vec3<i32>(floor(p)): one saturating round-down conversion (NaN -> 0).
+    const int x = __float2int_rd(r.px), y = __float2int_rd(r.py), z = __float2int_rd(r.pz);
+    const int d = (x ^ r.lx) | (y ^ r.ly) | (z ^ r.lz);
+    r.lx = x; r.ly = y; r.lz = z;
+    int lvl;
+    if (r.np == 3 && (d & ~7) == 0) lvl = 3;
+    else if (r.np >= 2 && (d & ~127) == 0) lvl = 4;
+    else if (r.np >= 1 && (d & ~4095) == 0) lvl = 5;
+    else lvl = 0;
+    uint32_t dist = 1;
+    if (lvl == 0) {  // get_vdb_leaf_from_nothing (:398-413): linear scan of the N5 origins
+        const int kx = x & ~4095, ky = y & ~4095, kz = z & ~4095;
+        r.np = 0;
+        for (uint32_t k = 0; k < g.n5; k++) {
+            const int4 o = __ldg(&g.o5[k]);
+            if (o.x == kx && o.y == ky && o.z == kz) {
+                r.i5 = k;
+                lvl = 5;
+                break;
+            }
+        }
+    }
+    if (lvl == 5) {  // get_vdb_leaf_from_node5 (:415-444)
+        const uint32_t off = ((((uint32_t)x >> 7) & 31u) << 10) | ((((uint32_t)y >> 7) & 31u) << 5) |
+                             (((uint32_t)z >> 7) & 31u);
+        const uint32_t w = __ldg(g.slot5 + ((size_t)r.i5 << 15) + off);
+        r.np = 1;
+        if (w & kChild) {
+            r.i4 = w & ~kChild;
+            lvl = 4;
+        } else {
+            dist = w;
+        }
+    }
+    if (lvl == 4) {  // get_vdb_leaf_from_node4 (:446-475)
+        const uint32_t off = ((((uint32_t)x >> 3) & 15u) << 8) | ((((uint32_t)y >> 3) & 15u) << 4) |
+                             (((uint32_t)z >> 3) & 15u);
+        const uint32_t w = __ldg(g.slot4 + ((size_t)r.i4 << 12) + off);
+        r.np = 2;
+        if (w & kChild) {
+            r.i3 = w & ~kChild;
+            lvl = 3;
+        } else {
+            dist = w;
+        }
+    }
+    if (lvl == 3) {  // get_vdb_leaf_from_node3 (:477-494)
+        const uint32_t off = (((uint32_t)x & 7u) << 6) | (((uint32_t)y & 7u) << 3) | ((uint32_t)z & 7u);
+        dist = __ldg(g.slot3 + ((size_t)r.i3 << 9) + off);
+        r.np = 3;
+    }
+    if (dist == 0u) return 0u;
+    // any(4096 < |p|); a NaN coordinate compares false, and fmaxf skips NaN.
+    if (4096.0f < fmaxf(fmaxf(fabsf(r.px), fabsf(r.py)), fabsf(r.pz))) return 1u;
+    // size = f32(dist) * scale[by num_parents] (:105-112)
+    const int sk = r.np == 3 ? 0 : r.np == 2 ? 3 : r.np == 1 ? 7 : 12;
+    const float size = __uint2float_rn(dist) * __int_as_float((127 + sk) << 23);
+    bool fast;
+    const float ys = rcp_size(dist, sk, &fast);
+    float qx, qy, qz;
+    if (fast && !(tiny_nonzero(r.px) || tiny_nonzero(r.py) || tiny_nonzero(r.pz))) {
+        qx = div_fast(r.px, size, ys);
+        qy = div_fast(r.py, size, ys);
+        qz = div_fast(r.pz, size, ys);
+    } else {
+        qx = __fdiv_rn(r.px, size);
+        qy = __fdiv_rn(r.py, size);
+        qz = __fdiv_rn(r.pz, size);
+    }
+    // tMax = idir * (size * step01 - (p - size * floor(p / size)))  (:78-80, :114);
+    // size * step01 is size or +0.
+    const float tx = r.ix * ((r.nx > 0.0f ? size : 0.0f) - (r.px - size * floorf(qx)));
+    const float ty = r.iy * ((r.ny > 0.0f ? size : 0.0f) - (r.py - size * floorf(qy)));
+    const float tz = r.iz * ((r.nz > 0.0f ? size : 0.0f) - (r.pz - size * floorf(qz)));
+    const float t = pmin(pmin(tx, ty), tz);
+    r.px = r.px + t * r.dx;
+    r.py = r.py + t * r.dy;
+    r.pz = r.pz + t * r.dz;
+    const bool mx = (tx <= ty) && (tx <= tz);
+    const bool my = (ty <= tz) && (ty <= tx);
+    const bool mz = (tz <= tx) && (tz <= ty);
+    r.mask = (mx ? 1u : 0u) | (my ? 2u : 0u) | (mz ? 4u : 0u);
+    // p += (4e-4 * step) * f32(mask): the addend is n or n * 0 (a signed zero).
+    r.px = r.px + (mx ? r.nx : r.nx * 0.0f);
+    r.py = r.py + (my ? r.ny : r.ny * 0.0f);
+    r.pz = r.pz + (mz ? r.nz : r.nz * 0.0f);
+    r.i++;
+    return 0xFFu;
+}
+
+__device__ __forceinline__ uint32_t ray_node(const Ray &r) {
+    return r.np == 3 ? r.i3 : r.np == 2 ? r.i4 : r.np == 1 ? r.i5 : 0xFFFFFFFFu;
+}
+
 struct March {
     F3 p;
     uint32_t state;  // 0 hit, 1 out of bounds, 2 step cap
@@ -73,106 +226,21 @@ struct March {
     uint32_t mask;   // bit0 x, bit1 y, bit2 z
 };
 
-// hdda_ray (raycast.comp.wgsl:84-126) with the cached descent of
-// get_vdb_leaf_from_{leaf,nothing,node5,node4,node3} (:360-494).
+// hdda_ray (raycast.comp.wgsl:84-126) run to completion.
 __device__ __forceinline__ March hdda(const DevGrid &g, F3 src, F3 dir) {
-    float px = src.x, py = src.y, pz = src.z;
-    const float sx = sign11(dir.x), sy = sign11(dir.y), sz = sign11(dir.z);
-    const float ax = pmax(0.0f, sx), ay = pmax(0.0f, sy), az = pmax(0.0f, sz);
-    const float ix = __frcp_rn(dir.x), iy = __frcp_rn(dir.y), iz = __frcp_rn(dir.z);
-    uint32_t np = 0, i5 = 0, i4 = 0, i3 = 0, mask = 0;
-    int o5x = 0, o5y = 0, o5z = 0, o4x = 0, o4y = 0, o4z = 0, o3x = 0, o3y = 0, o3z = 0;
-    March out;
-    for (uint32_t i = 0; i < kMaxSteps; i++) {
-        const int x = f2i(floorf(px)), y = f2i(floorf(py)), z = f2i(floorf(pz));
-        // get_vdb_leaf_from_leaf: deepest cached node whose origin contains pos.
-        int lvl;
-        if (np == 3 && (x & ~7) == o3x && (y & ~7) == o3y && (z & ~7) == o3z) lvl = 3;
-        else if (np >= 2 && (x & ~127) == o4x && (y & ~127) == o4y && (z & ~127) == o4z) lvl = 4;
-        else if (np >= 1 && (x & ~4095) == o5x && (y & ~4095) == o5y && (z & ~4095) == o5z) lvl = 5;
-        else lvl = 0;
-        uint32_t dist = 1;
-        if (lvl == 0) {  // get_vdb_leaf_from_nothing: scan the N5 origins
-            const int kx = x & ~4095, ky = y & ~4095, kz = z & ~4095;
-            np = 0;
-            for (uint32_t k = 0; k < g.n5; k++) {
-                const int4 o = __ldg(&g.o5[k]);
-                if (o.x == kx && o.y == ky && o.z == kz) {
-                    i5 = k;
-                    o5x = kx; o5y = ky; o5z = kz;
-                    lvl = 5;
-                    break;
-                }
-            }
-        }
-        if (lvl == 5) {
-            const uint32_t off = ((((uint32_t)x & 4095u) >> 7) << 10) | ((((uint32_t)y & 4095u) >> 7) << 5) |
-                                 (((uint32_t)z & 4095u) >> 7);
-            const uint32_t w = __ldg(&g.slot5[(size_t)i5 * 32768u + off]);
-            np = 1;
-            if (w & kChild) {
-                i4 = w & ~kChild;
-                o4x = x & ~127; o4y = y & ~127; o4z = z & ~127;
-                lvl = 4;
-            } else {
-                dist = w;
-            }
-        }
-        if (lvl == 4) {
-            const uint32_t off = ((((uint32_t)x & 127u) >> 3) << 8) | ((((uint32_t)y & 127u) >> 3) << 4) |
-                                 (((uint32_t)z & 127u) >> 3);
-            const uint32_t w = __ldg(&g.slot4[(size_t)i4 * 4096u + off]);
-            np = 2;
-            if (w & kChild) {
-                i3 = w & ~kChild;
-                o3x = x & ~7; o3y = y & ~7; o3z = z & ~7;
-                lvl = 3;
-            } else {
-                dist = w;
-            }
-        }
-        if (lvl == 3) {
-            const uint32_t off = (((uint32_t)x & 7u) << 6) | (((uint32_t)y & 7u) << 3) | ((uint32_t)z & 7u);
-            dist = __ldg(&g.slot3[(size_t)i3 * 512u + off]);
-            np = 3;
-        }
-        if (dist == 0u) {
-            out.state = 0;
-            out.i = i;
-            goto done;
-        }
-        if (4096.0f < fabsf(px) || 4096.0f < fabsf(py) || 4096.0f < fabsf(pz)) {
-            out.state = 1;
-            out.i = i;
-            goto done;
-        }
-        {
-            float size = __uint2float_rn(dist);
-            size = size * (np == 3 ? 1.0f : np == 2 ? 8.0f : np == 1 ? 128.0f : 4096.0f);
-            const float tx = ix * (size * ax - (px - size * floorf(__fdiv_rn(px, size))));
-            const float ty = iy * (size * ay - (py - size * floorf(__fdiv_rn(py, size))));
-            const float tz = iz * (size * az - (pz - size * floorf(__fdiv_rn(pz, size))));
-            const float t = pmin(pmin(tx, ty), tz);
-            px = px + t * dir.x;
-            py = py + t * dir.y;
-            pz = pz + t * dir.z;
-            const bool mx = (tx <= ty) && (tx <= tz);
-            const bool my = (ty <= tz) && (ty <= tx);
-            const bool mz = (tz <= tx) && (tz <= ty);
-            mask = (mx ? 1u : 0u) | (my ? 2u : 0u) | (mz ? 4u : 0u);
-            px = px + (4e-4f * sx) * (mx ? 1.0f : 0.0f);
-            py = py + (4e-4f * sy) * (my ? 1.0f : 0.0f);
-            pz = pz + (4e-4f * sz) * (mz ? 1.0f : 0.0f);
-        }
+    Ray r;
+    ray_init(r, src, dir);
+    uint32_t st;
+    while ((st = ray_step(g, r)) == 0xFFu) {
     }
-    out.state = 2;
-    out.i = kMaxSteps;
-done:
-    out.p = f3(px, py, pz);
-    out.np = np;
-    out.node = np == 3 ? i3 : np == 2 ? i4 : np == 1 ? i5 : 0xFFFFFFFFu;
-    out.mask = mask;
-    return out;
+    March m;
+    m.p = f3(r.px, r.py, r.pz);
+    m.state = st;
+    m.np = r.np;
+    m.node = ray_node(r);
+    m.i = r.i;
+    m.mask = r.mask;
+    return m;
 }
 
 __device__ __forceinline__ F3 maskf(uint32_t m) {
@@ -194,13 +262,9 @@ __device__ __forceinline__ F3 wall_colour(F3 N) {  // :300-305 / :333-338
     return r;
 }
 
-struct ShadowRec {
-    uint32_t traced, state, steps;
-};
-
 // Lit material colour shared by mode 4 and reflect_ray2/1 (:199-208, :280-290, :317-325).
-__device__ __forceinline__ F3 lit_colour(const DevGrid &g, const wx_state_uniform &s, const March &h,
-                                         F3 step, F3 N) {
+__device__ __forceinline__ F3 lit_colour(const DevGrid &g, const wx_state_uniform &s, const March &h, F3 step,
+                                         F3 N) {
     const F3 sun = f3(s.sun_dir[0], s.sun_dir[1], s.sun_dir[2]);
     const F3 sc = f3(s.sun_color[0], s.sun_color[1], s.sun_color[2]);
     float I = (s.sun_color[3] * kKd) * dot3(-sun, N);
@@ -213,7 +277,7 @@ __device__ __forceinline__ F3 lit_colour(const DevGrid &g, const wx_state_unifor
     return base + I * sc;
 }
 
-__device__ F3 reflect_ray1(const DevGrid &g, const wx_state_uniform &s, F3 src, F3 dir) {  // :311-342
+__device__ __noinline__ F3 reflect_ray1(const DevGrid &g, const wx_state_uniform &s, F3 src, F3 dir) {  // :311-342
     const March h = hdda(g, src, dir);
     const F3 step = step3(dir);
     if (h.state == 0u) return lit_colour(g, s, h, step, normalize3((-step) * maskf(h.mask)));
@@ -221,7 +285,7 @@ __device__ F3 reflect_ray1(const DevGrid &g, const wx_state_uniform &s, F3 src, 
     return dir;
 }
 
-__device__ F3 reflect_ray2(const DevGrid &g, const wx_state_uniform &s, F3 src, F3 dir) {  // :267-309
+__device__ __noinline__ F3 reflect_ray2(const DevGrid &g, const wx_state_uniform &s, F3 src, F3 dir) {  // :267-309
     const March h = hdda(g, src, dir);
     const F3 step = step3(dir);
     if (h.state == 0u) {
@@ -239,24 +303,31 @@ __device__ F3 reflect_ray2(const DevGrid &g, const wx_state_uniform &s, F3 src, 
 
 __device__ __forceinline__ bool grid_line(float f, float m) { return fmodf(f, m) == 0.0f; }
 
-// ray_trace (:152-265) for the primary ray; also returns its march and shadow record.
-__device__ __forceinline__ F3 ray_trace(const DevGrid &g, const wx_state_uniform &s, F3 eye, F3 dir,
-                                        March &hit, ShadowRec &sh) {
-    hit = hdda(g, eye, dir);
+// The `grid` tint of ray_trace (:157-166).
+__device__ __forceinline__ F3 grid_tint(const wx_state_uniform &s, F3 p) {
+    const float fx = floorf(p.x), fy = floorf(p.y), fz = floorf(p.z);
+    if (s.show_345[2] == 1u && (grid_line(fx, 4096.0f) || grid_line(fy, 4096.0f) || grid_line(fz, 4096.0f)))
+        return f3(-0.3f, -0.3f, 1.0f);
+    if (s.show_345[1] == 1u && (grid_line(fx, 128.0f) || grid_line(fy, 128.0f) || grid_line(fz, 128.0f)))
+        return f3(0.6f, -0.2f, -0.2f);
+    if (s.show_345[0] == 1u && (grid_line(fx, 8.0f) || grid_line(fy, 8.0f) || grid_line(fz, 8.0f)))
+        return f3(-0.1f, 0.5f, 0.3f);
+    return splat(0.0f);
+}
+
+// Colour of a finished primary ray for modes 0-2 and the non-lit part of
+// modes 0-3 (:156-194 for state 0, :231-262 for state 1, :264 otherwise).
+// For mode 3 with a hit, *need_shadow tells the caller to trace the shadow
+// ray (:188-193); the colour returned is then I_a + I_d (the unshadowed case)
+// and *shadowed_colour receives I_a.
+__device__ __forceinline__ F3 primary_colour(const wx_state_uniform &s, const March &hit, F3 dir, bool *need_shadow,
+                                             F3 *shadowed_colour, F3 *shadow_src) {
     const F3 step = step3(dir);
     const uint32_t mode = s.render_mode[0];
-    sh.traced = 0;
+    *need_shadow = false;
     if (hit.state == 0u) {
-        F3 grid = splat(0.0f);
-        const float fx = floorf(hit.p.x), fy = floorf(hit.p.y), fz = floorf(hit.p.z);
-        if (s.show_345[2] == 1u && (grid_line(fx, 4096.0f) || grid_line(fy, 4096.0f) || grid_line(fz, 4096.0f)))
-            grid = f3(-0.3f, -0.3f, 1.0f);
-        else if (s.show_345[1] == 1u &&
-                 (grid_line(fx, 128.0f) || grid_line(fy, 128.0f) || grid_line(fz, 128.0f)))
-            grid = f3(0.6f, -0.2f, -0.2f);
-        else if (s.show_345[0] == 1u && (grid_line(fx, 8.0f) || grid_line(fy, 8.0f) || grid_line(fz, 8.0f)))
-            grid = f3(-0.1f, 0.5f, 0.3f);
         const F3 m = maskf(hit.mask);
+        const F3 grid = grid_tint(s, hit.p);
         if (mode == 1u) return (grid + splat(0.1f)) + m * splat(0.4f);
         if (mode == 2u) {
             const float t = __fdiv_rn(__uint2float_rn(hit.i), 200.0f);
@@ -270,21 +341,11 @@ __device__ __forceinline__ F3 ray_trace(const DevGrid &g, const wx_state_uniform
             const F3 I_d = ((kKd * sc) * f3(0.4f, 0.2f, 0.2f)) * LN;
             const F3 I_a = (kKa * f3(0.4f, 0.4f, 0.3f)) * f3(0.4f, 0.2f, 0.2f);
             if (LN != 0.0f) {
-                const March shd = hdda(g, hit.p - (4e-2f * step) * m, -sun);
-                sh.traced = 1;
-                sh.state = shd.state;
-                sh.steps = shd.i;
-                if (shd.state == 0u) return I_a;
+                *need_shadow = true;
+                *shadowed_colour = I_a;
+                *shadow_src = hit.p - (4e-2f * step) * m;
             }
             return I_a + I_d;
-        }
-        if (mode == 4u) {
-            const F3 N = normalize3((-step) * m);
-            const F3 mcol = lit_colour(g, s, hit, step, N);
-            const F3 rdir = normalize3(dir - (2.0f * N) * dot3(dir, N));
-            const F3 rsrc = hit.p - (4e-2f * step) * m;
-            const F3 rcol = reflect_ray2(g, s, rsrc, rdir);
-            return mix3(mcol, rcol, kReflect);
         }
         const F3 a = m * f3(0.2f, 0.2f, 0.3f);  // mode 0 and default
         return grid + splat((a.x + a.y) + a.z);
@@ -296,46 +357,55 @@ __device__ __forceinline__ F3 ray_trace(const DevGrid &g, const wx_state_uniform
             const F3 a = m * f3(0.04f, 0.08f, 0.12f);
             return mix3(f3(0.72f, 1.0f, 0.99f), f3(1.0f, 0.0f, 0.0f), t) + splat((a.x + a.y) + a.z);
         }
-        if (mode == 4u) {
-            const F3 N = normalize3((-step) * m);
-            const F3 Np = f3(pmax(0.0f, N.x), pmax(0.0f, N.y), pmax(0.0f, N.z));
-            const F3 Nn = -f3(pmin(0.0f, N.x), pmin(0.0f, N.y), pmin(0.0f, N.z));
-            const float ty = __fdiv_rn(hit.p.y, 4096.0f);
-            const float w1 = kWall * 0.1f;
-            F3 r = mix3(f3(kWall, 0.0f, 0.0f), f3(w1, 0.0f, 0.0f), ty) * Np.x;
-            r = r + f3(0.0f, kWall, 0.0f) * Np.y;
-            r = r + mix3(f3(0.0f, 0.0f, kWall), f3(0.0f, 0.0f, w1), ty) * Np.z;
-            r = r + mix3(f3(kWall, kWall, 0.0f), f3(w1, w1, 0.0f), ty) * Nn.x;
-            r = r + f3(0.0f, kWall, kWall) * Nn.y;
-            r = r + mix3(f3(kWall, 0.0f, kWall), f3(w1, 0.0f, w1), ty) * Nn.z;
-            return r;
-        }
         const F3 a = m * f3(0.01f, 0.02f, 0.03f);
         return splat(0.0f) + splat((a.x + a.y) + a.z);
     }
     return dir;
 }
 
-// cp_main (raycast.comp.wgsl:60-68) for pixel (gx, gy): colour and hit record.
-__device__ __forceinline__ void shade_pixel(const DevGrid &g, const wx_state_uniform &s, uint32_t gx,
-                                            uint32_t gy, uint32_t &rgba, wx_hit &rec) {
+// Glossy mode (:195-224 for state 0, :246-257 for state 1), up to six rays.
+__device__ __noinline__ F3 glossy_colour(const DevGrid &g, const wx_state_uniform &s, const March &hit, F3 dir) {
+    const F3 step = step3(dir);
+    const F3 m = maskf(hit.mask);
+    const F3 N = normalize3((-step) * m);
+    if (hit.state == 0u) {
+        const F3 mcol = lit_colour(g, s, hit, step, N);
+        const F3 rdir = normalize3(dir - (2.0f * N) * dot3(dir, N));
+        const F3 rsrc = hit.p - (4e-2f * step) * m;
+        const F3 rcol = reflect_ray2(g, s, rsrc, rdir);
+        return mix3(mcol, rcol, kReflect);
+    }
+    if (hit.state == 1u) {
+        const F3 Np = f3(pmax(0.0f, N.x), pmax(0.0f, N.y), pmax(0.0f, N.z));
+        const F3 Nn = -f3(pmin(0.0f, N.x), pmin(0.0f, N.y), pmin(0.0f, N.z));
+        const float ty = __fdiv_rn(hit.p.y, 4096.0f);
+        const float w1 = kWall * 0.1f;
+        F3 r = mix3(f3(kWall, 0.0f, 0.0f), f3(w1, 0.0f, 0.0f), ty) * Np.x;
+        r = r + f3(0.0f, kWall, 0.0f) * Np.y;
+        r = r + mix3(f3(0.0f, 0.0f, kWall), f3(0.0f, 0.0f, w1), ty) * Np.z;
+        r = r + mix3(f3(kWall, kWall, 0.0f), f3(w1, w1, 0.0f), ty) * Nn.x;
+        r = r + f3(0.0f, kWall, kWall) * Nn.y;
+        r = r + mix3(f3(kWall, 0.0f, kWall), f3(w1, 0.0f, w1), ty) * Nn.z;
+        return r;
+    }
+    return dir;
+}
+
+// cp_main's ray (raycast.comp.wgsl:62-63) for pixel (gx, gy).
+__device__ __forceinline__ F3 primary_dir(const wx_state_uniform &s, uint32_t gx, uint32_t gy) {
     const float px = __uint2float_rn(gx) + 0.001f, py = __uint2float_rn(gy) + 0.001f;
-    const F3 r = f3((px * s.u[0] + py * s.mv[0]) + s.wp[0], (px * s.u[1] + py * s.mv[1]) + s.wp[1],
-                    (px * s.u[2] + py * s.mv[2]) + s.wp[2]);
-    const F3 dir = normalize3(r);
-    const F3 eye = f3(s.eye[0], s.eye[1], s.eye[2]);
-    March hit;
-    ShadowRec sh;
-    const F3 c = ray_trace(g, s, eye, dir, hit, sh);
-    rgba = unorm8(c.x) | (unorm8(c.y) << 8) | (unorm8(c.z) << 16) | (255u << 24);
-    rec.p[0] = hit.p.x;
-    rec.p[1] = hit.p.y;
-    rec.p[2] = hit.p.z;
-    rec.t = dot3(hit.p - eye, dir);
-    rec.node = hit.node;
-    rec.info = hit.state | (hit.np << 2) | (hit.mask << 4) | (hit.i << 8);
-    rec.shadow = sh.traced ? (1u | (sh.state << 1) | (sh.steps << 8)) : 0u;
-    rec.reserved = 0u;
+    return normalize3(f3((px * s.u[0] + py * s.mv[0]) + s.wp[0], (px * s.u[1] + py * s.mv[1]) + s.wp[1],
+                         (px * s.u[2] + py * s.mv[2]) + s.wp[2]));
+}
+
+__device__ __forceinline__ uint32_t pack_rgba(F3 c) {
+    return unorm8(c.x) | (unorm8(c.y) << 8) | (unorm8(c.z) << 16) | (255u << 24);
+}
+
+__device__ __forceinline__ void store_hit(wx_hit *h, F3 p, float t, uint32_t node, uint32_t info, uint32_t shadow) {
+    uint4 *q = reinterpret_cast<uint4 *>(h);
+    q[0] = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), __float_as_uint(p.z), __float_as_uint(t));
+    q[1] = make_uint4(node, info, shadow, 0u);
 }
 
 }  // namespace wxd

@@ -1,0 +1,50 @@
+// wx_kernels.h — host-side view of the kernels in kernels.cu (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "woxel_gb300.h"
+
+namespace wxk {
+
+struct DevGrid {  // same layout as wxd::DevGrid
+    const int4 *o5;
+    const uint32_t *slot5;
+    const uint32_t *slot4;
+    const uint32_t *slot3;
+    uint32_t n5;
+};
+
+// One frame of one grid: the unit the persistent kernels draw ray tiles from.
+struct Job {
+    DevGrid g;
+    uint32_t width, height;
+    uint32_t tile_w, tile_h;       // pixel tile of one warp (tile_w * tile_h = 32)
+    uint32_t tiles_x, tiles;       // tiles per row / per frame over the dispatched region
+    uint32_t tile_begin, pad;      // first global tile id of this job
+    uint32_t *rgba;
+    wx_hit *hits;
+    wx_state_uniform s;
+};
+
+struct Tuning {
+    int kernel = 0;            // 0 persistent warps on a tile queue, 1 one warp per tile in launch order
+    int warps_per_block = 4;   // 1..16
+    int blocks_per_sm = 0;     // 0 = as many as fit
+    int tile_w = 8;            // 4, 8, 16 or 32 pixels wide (x 32/tile_w high)
+};
+
+cudaError_t init_device_tables();
+int max_blocks_per_sm(int kernel, bool batched, int warps_per_block);
+cudaError_t launch_pixel(const Job &job, const Tuning &t, cudaStream_t st);
+cudaError_t launch_persistent(const Job &job, uint32_t *ctr, const Tuning &t, int num_sms, cudaStream_t st);
+cudaError_t launch_batched(const Job *jobs_dev, uint32_t njobs, uint32_t total_tiles, uint32_t *ctr,
+                           const Tuning &t, int num_sms, cudaStream_t st);
+// Exhaustive check of the fast floor-division path against IEEE division:
+// every odd m < max_m and every significand of [1,2) and [-2,-1).
+// out[0] = mismatch count, out[1] = first mismatching m, out[2] = its x bits.
+cudaError_t check_division(uint32_t max_m, unsigned long long *out_dev, cudaStream_t st);
+
+}  // namespace wxk
