@@ -168,6 +168,31 @@ int wx_batch_launch(wx_batch *batch, void *stream);
 int wx_batch_info(const wx_batch *batch, uint32_t *frames, uint32_t *tiles, uint64_t *rays);
 int wx_batch_destroy(wx_batch *batch);
 
+/* ---- batched rendering that allocates nothing (no counterpart in the
+ * reference) ----
+ * For callers that must not allocate device memory while rendering: engines
+ * that reserve all GPU memory at start-up and forbid cudaMalloc afterwards, or
+ * code on a deadline (a frame callback) where an allocation could stall or
+ * fail. It renders like wx_render_batch (same results per frame) but needs no
+ * context and calls no allocating routine: its work-queue counter and frame
+ * table live in one fixed device array of WX_NOALLOC_SCRATCH_BYTES that the
+ * library declares statically, so every GPU that loads the library holds that
+ * memory until the process exits. The caller passes the grids and the device
+ * output buffers.
+ * Limits: at most WX_NOALLOC_MAX_FRAMES frames per call (more is rejected with
+ * WX_ERR_INVALID); all grids on one device; outputs in device memory; default
+ * launch shape (8x4 tiles).
+ * The first call on a device does a one-time set-up on that device (it looks
+ * up the array's device address and loads the kernels' division table): make
+ * that first call before any stream capture. Every call reuses the same array
+ * and clears its counter, so calls that overlap on the GPU (on different
+ * streams, or from other host threads before earlier work finished) race; the
+ * caller must serialise them. The call blocks until earlier work on `stream`
+ * is done, because the frame table is copied from pageable host memory. */
+#define WX_NOALLOC_MAX_FRAMES 256
+#define WX_NOALLOC_SCRATCH_BYTES 88320 /* 256 + 256 frames x 344-byte table entries */
+int wx_render_batch_noalloc(const wx_frame *frames, uint32_t n, void *stream);
+
 /* Exhaustive GPU check of the kernels' fast floor(p / size) path against IEEE
  * division: every odd divisor m < max_m (<= 4096) and every significand of
  * [1,2) and [-2,-1). out = {mismatches, first bad m, its x bits}. */

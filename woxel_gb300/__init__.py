@@ -294,6 +294,20 @@ class Context:
         return Batch(self, out.value, [f[0] for f in frames])
 
 
+NOALLOC_MAX_FRAMES = 256
+
+
+def render_batch_noalloc(frames: Sequence, stream=None) -> None:
+    """wx_render_batch_noalloc: a batch rendered without any allocation or context.
+
+    For callers that cannot allocate device memory while rendering; scratch is a
+    fixed 88,320-byte device array inside the library (at most 256 frames a call).
+    The first call on a device sets that device up; overlapping calls race.
+    """
+    arr = Context._frames(frames)
+    check(lib().wx_render_batch_noalloc(arr, len(frames), None if stream is None else int(stream)))
+
+
 class Batch:
     """A batched launch captured in a CUDA graph (wx_batch_create / wx_batch_launch)."""
 

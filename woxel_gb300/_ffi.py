@@ -71,6 +71,7 @@ SIGNATURES = {
     "wx_batch_launch": (INT, [P, P]),
     "wx_batch_info": (INT, [P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U64)]),
     "wx_batch_destroy": (INT, [P]),
+    "wx_render_batch_noalloc": (INT, [C.POINTER(wx_frame), U32, P]),
     "wx_check_division": (INT, [P, U32, C.POINTER(U64)]),
     "wx_state_build": (INT, [P, P, P, F32, F32, F32, U32, P, P, P, F32, C.POINTER(wx_state_uniform)]),
     "wx_sun_default": (None, [P, P, P]),

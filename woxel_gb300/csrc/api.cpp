@@ -160,6 +160,13 @@ wxk::Job make_job(const wx_grid *grid, const wx_state_uniform &s, uint32_t width
 
 }  // namespace
 
+bool wxk::grid_device_view(const wx_grid *grid, wxk::DevGrid *out, int *device) {
+    if (!grid) return false;
+    *out = grid->g;
+    *device = grid->device;
+    return true;
+}
+
 extern "C" {
 
 const char *wx_status_string(int status) {

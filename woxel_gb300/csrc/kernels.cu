@@ -11,7 +11,10 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
+#include <mutex>
 
+#include "wx_common.h"
 #include "wx_device.cuh"
 #include "wx_kernels.h"
 
@@ -187,3 +190,144 @@ cudaError_t check_division(uint32_t max_m, unsigned long long *out_dev, cudaStre
 }
 
 }  // namespace wxk
+
+// ---------------------------------------------------------------------------
+// Batched rendering for callers that must not allocate (wx_render_batch_noalloc).
+//
+// Some callers cannot allocate device memory at render time: engines that
+// reserve all GPU memory at start-up and forbid cudaMalloc afterwards, or code
+// running where an allocation could stall or fail (a frame callback with a
+// deadline). wx_render_batch needs a context whose scratch (queue counters,
+// frame table) comes from cudaMalloc. This entry point instead keeps its
+// scratch in the fixed device array below, which the library declares
+// statically: every GPU that loads the library holds these 88,320 bytes until
+// the process exits. Layout: the tile-queue counter at byte 0, the frame
+// (job) table from byte 256, room for WX_NOALLOC_MAX_FRAMES frames.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoallocJobsOffset = 256;
+constexpr size_t kNoallocBytes = kNoallocJobsOffset + (size_t)WX_NOALLOC_MAX_FRAMES * sizeof(Job);
+static_assert(kNoallocBytes == WX_NOALLOC_SCRATCH_BYTES, "scratch size stated in woxel_gb300.h");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+// Per-device state of the one-time set-up (host side).
+struct NoallocDevice {
+    bool ready = false;
+    unsigned char *scratch = nullptr;  // device address of g_noalloc_scratch on this device
+    int num_sms = 0;
+};
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mu;                     // guards the set-up and the host frame table
+NoallocDevice g_noalloc_dev[kNoallocMaxDevices];
+Job g_noalloc_table[WX_NOALLOC_MAX_FRAMES];  // host staging of the frame table (static, not heap)
+
+int noalloc_fail(int code, const char *msg) {
+    wx::set_thread_error(msg);
+    return code;
+}
+
+// Once per device, with that device current: find the array's device address
+// (host code cannot use the symbol itself) and load the division table.
+int noalloc_setup(int device, NoallocDevice **out) {
+    NoallocDevice &d = g_noalloc_dev[device];
+    if (!d.ready) {
+        cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void **>(&d.scratch), g_noalloc_scratch);
+        if (e != cudaSuccess) return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: cudaGetSymbolAddress failed");
+        if ((e = wxk::init_device_tables()) != cudaSuccess)
+            return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: loading the division table failed");
+        if ((e = cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
+            return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: cudaDeviceGetAttribute failed");
+        d.ready = true;
+    }
+    *out = &d;
+    return WX_OK;
+}
+
+bool noalloc_device_memory(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int noalloc_render(int device, const wx_frame *frames, uint32_t n, cudaStream_t st) {
+    NoallocDevice *d = nullptr;
+    int rc = noalloc_setup(device, &d);
+    if (rc != WX_OK) return rc;
+    // Frame table with the default launch shape (8x4 tiles), as wx_render_batch builds it.
+    const wxk::Tuning tuning;
+    uint32_t njobs = 0;
+    uint64_t tiles = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const wx_frame &f = frames[i];
+        Job &j = g_noalloc_table[njobs];
+        memset(&j, 0, sizeof j);
+        int gdev = -1;
+        if (!f.rgba8 || !wxk::grid_device_view(f.grid, &j.g, &gdev))
+            return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: frame with a NULL grid or rgba8");
+        if (gdev != device) return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: grids on different devices");
+        if (((uintptr_t)f.rgba8 & 3) || ((uintptr_t)f.hits & 15))
+            return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: rgba8 must be 4-byte and hits 16-byte aligned");
+        if (!noalloc_device_memory(f.rgba8) || (f.hits && !noalloc_device_memory(f.hits)))
+            return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: outputs must be device memory");
+        if ((uint64_t)f.width * f.height >= (1ull << 32))
+            return noalloc_fail(WX_ERR_UNSUPPORTED, "wx_render_batch_noalloc: frame too large");
+        j.width = f.width;
+        j.height = f.height;
+        j.tile_w = (uint32_t)tuning.tile_w;
+        j.tile_h = 32u / j.tile_w;
+        j.tiles_x = ((f.width & ~7u) + j.tile_w - 1) / j.tile_w;
+        j.tiles = j.tiles_x * (((f.height & ~3u) + j.tile_h - 1) / j.tile_h);
+        j.tile_begin = (uint32_t)tiles;
+        j.rgba = reinterpret_cast<uint32_t *>(f.rgba8);
+        j.hits = f.hits;
+        j.s = f.state;
+        if (j.tiles == 0) continue;  // nothing dispatched; keep job tile ranges non-empty
+        tiles += j.tiles;
+        njobs++;
+        if (tiles >= (1ull << 31)) return noalloc_fail(WX_ERR_UNSUPPORTED, "wx_render_batch_noalloc: too many tiles");
+    }
+    if (njobs == 0) return WX_OK;
+    unsigned char *scratch = d->scratch;
+    Job *jobs_dev = reinterpret_cast<Job *>(scratch + kNoallocJobsOffset);
+    uint32_t *counter = reinterpret_cast<uint32_t *>(scratch);
+    // Pageable source: the call returns once the table has been consumed, so
+    // the static host table can be reused by the next call.
+    cudaError_t e = cudaMemcpyAsync(jobs_dev, g_noalloc_table, njobs * sizeof(Job), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: frame table copy failed");
+    wxk::Tuning t;  // defaults; launch_batched clears the counter (it keeps the last call's value otherwise)
+    e = wxk::launch_batched(jobs_dev, njobs, (uint32_t)tiles, counter, t, d->num_sms, st);
+    if (e != cudaSuccess) return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: launch failed");
+    return WX_OK;
+}
+
+}  // namespace
+
+extern "C" int wx_render_batch_noalloc(const wx_frame *frames, uint32_t n, void *stream) {
+    if (n == 0) return WX_OK;
+    if (!frames) return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: frames is NULL");
+    if (n > WX_NOALLOC_MAX_FRAMES)
+        return noalloc_fail(WX_ERR_INVALID,
+                            "wx_render_batch_noalloc: more than WX_NOALLOC_MAX_FRAMES (256) frames in one call");
+    wxk::DevGrid g;
+    int device = -1;
+    if (!wxk::grid_device_view(frames[0].grid, &g, &device))
+        return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: frame 0 has a NULL grid");
+    if (device < 0 || device >= kNoallocMaxDevices)
+        return noalloc_fail(WX_ERR_UNSUPPORTED, "wx_render_batch_noalloc: device index above 63");
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: cudaGetDevice failed");
+    if (prev != device && cudaSetDevice(device) != cudaSuccess)
+        return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: cudaSetDevice failed");
+    int rc;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        rc = noalloc_render(device, frames, n, static_cast<cudaStream_t>(stream));
+    }
+    if (prev != device) cudaSetDevice(prev);
+    return rc;
+}

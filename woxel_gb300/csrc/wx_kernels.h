@@ -42,6 +42,9 @@ cudaError_t launch_pixel(const Job &job, const Tuning &t, cudaStream_t st);
 cudaError_t launch_persistent(const Job &job, uint32_t *ctr, const Tuning &t, int num_sms, cudaStream_t st);
 cudaError_t launch_batched(const Job *jobs_dev, uint32_t njobs, uint32_t total_tiles, uint32_t *ctr,
                            const Tuning &t, int num_sms, cudaStream_t st);
+// Device pools and device of a grid handle (defined in api.cpp); false for NULL.
+bool grid_device_view(const wx_grid *grid, DevGrid *out, int *device);
+
 // Exhaustive check of the fast floor-division path against IEEE division:
 // every odd m < max_m and every significand of [1,2) and [-2,-1).
 // out[0] = mismatch count, out[1] = first mismatching m, out[2] = its x bits.
