@@ -127,6 +127,23 @@ def test_edge_cameras(cuda_ctx, sphere64):
             compare(rg, hg, ro, ho, label=f"eye{eye}/mode{mode}")
 
 
+def test_zero_direction_components(cuda_ctx, sphere64):
+    """Rays with an exactly-zero direction component (1/dir = inf) take the NaN-aware step."""
+    _, view, grid = sphere64
+    w, h = 64, 64
+    st = wx.state_build(eye=(0.5, 0.0, 150.0), target=(0, 0, 0), aspect=1.0, fovy=60.0, width=float(w), mode=3,
+                        sun=((0.0, -1.0, 0.0), (1.0, 0.8, 0.6), 1.0))
+    # Hand-made ray basis: dir = (x - 32, 0, -40) for every pixel, so dir.y == 0 exactly.
+    for i in range(4):
+        st.u[i], st.mv[i], st.wp[i] = (1.0, 0.0, 0.0, 0.0)[i], 0.0, (-32.0, 0.0, -40.0, 0.0)[i]
+    for mode in (0, 3, 4):
+        st.render_mode[0] = mode
+        rg, hg = gpu_render(cuda_ctx, grid, st, w, h)
+        ro, ho = oracle_render(view, st, w, h)
+        compare(rg, hg, ro, ho, label=f"zero-dir/mode{mode}")
+    assert (wx.hit_fields(hg)["state"] == 0).any()
+
+
 def test_empty_grid(cuda_ctx):
     topo = wx.Topology.from_voxels(np.zeros((0, 3), np.int32))
     assert topo.counts == (0, 0, 0)

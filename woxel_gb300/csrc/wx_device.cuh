@@ -45,16 +45,14 @@ __device__ __forceinline__ float sign11(float x) { return x < 0.0f ? -1.0f : 1.0
 // bit-identical to __fdiv_rn except that a zero quotient may come out +0 for
 // p = -0; the march cannot observe that sign (mod = p - size*floor(q) enters
 // only size*step01 - mod, where +0 and -0 give the same value). Other cases
-// (m >= 4096, or 0 < |p| < 2^-64 where q0 could underflow) take __fdiv_rn.
+// (m >= 4096, or a coordinate with |p| < 2^-64, where q0 could underflow)
+// take __fdiv_rn.
 __device__ __forceinline__ float rcp_size(uint32_t dist, int sk, bool *fast) {
     const int tz = __ffs((int)dist) - 1;  // dist >= 1, so k = tz + sk <= 43
     const uint32_t m = dist >> tz;
     *fast = m < 2u * kRcpOdd;
     const float r = __ldg(&g_rcp_odd[(*fast ? m : 1u) >> 1]);
     return r * __int_as_float((127 - tz - sk) << 23);
-}
-__device__ __forceinline__ bool tiny_nonzero(float p) {  // 0 < |p| < 2^-64
-    return (__float_as_uint(p) & 0x7FFFFFFFu) - 1u < 0x1F7FFFFFu;
 }
 __device__ __forceinline__ float div_fast(float p, float size, float y) {
     const float q0 = p * y;
@@ -95,13 +93,14 @@ __device__ __forceinline__ uint32_t unorm8(float x) {
 // pool indices of the cached N5/N4/N3 plus the voxel of the previous lookup:
 // that voxel lies inside every cached node (levels 1..np), so "pos is in the
 // cached node of side S" is ((x ^ lx) | (y ^ ly) | (z ^ lz)) & ~(S - 1) == 0.
-// Per-ray constants: idir = 1/dir, and n = 4e-4 * sign11(dir), the nudge of
-// :122 (step01 = max(0, sign11(dir)) is n > 0).
+// Per-ray constants: idir = 1/dir and step01 = max(0, sign11(dir)) (:86-88).
+// The nudge 4e-4 * step of :122 is (step01 - 0.5) * RN(8e-4), exactly
+// +-RN(4e-4) because RN commutes with scaling by two.
 struct Ray {
     float px, py, pz;
     float dx, dy, dz;
     float ix, iy, iz;
-    float nx, ny, nz;
+    float ax, ay, az;  // step01
     int lx, ly, lz;
     uint32_t np, i5, i4, i3;
     uint32_t mask, i;
@@ -111,26 +110,37 @@ __device__ __forceinline__ void ray_init(Ray &r, F3 src, F3 dir) {
     r.px = src.x; r.py = src.y; r.pz = src.z;
     r.dx = dir.x; r.dy = dir.y; r.dz = dir.z;
     r.ix = __frcp_rn(dir.x); r.iy = __frcp_rn(dir.y); r.iz = __frcp_rn(dir.z);
-    r.nx = 4e-4f * sign11(dir.x); r.ny = 4e-4f * sign11(dir.y); r.nz = 4e-4f * sign11(dir.z);
+    r.ax = pmax(0.0f, sign11(dir.x)); r.ay = pmax(0.0f, sign11(dir.y)); r.az = pmax(0.0f, sign11(dir.z));
     r.lx = r.ly = r.lz = 0;
     r.np = 0; r.i5 = r.i4 = r.i3 = 0;
     r.mask = 0;
     r.i = 0;
 }
 
+// A ray needs the NaN-aware step when 1/dir can be infinite (a direction
+// component of magnitude below 2^-126, zero, or NaN): only then can
+// idir * (size*step01 - mod) be inf * 0 = NaN. Otherwise every tMax is a
+// number and min/argmin need no NaN handling.
+__device__ __forceinline__ bool ray_needs_nan_checks(F3 dir) {
+    return !(fminf(fminf(fabsf(dir.x), fabsf(dir.y)), fabsf(dir.z)) >= 0x1p-126f);
+}
+
 // One loop iteration of hdda_ray. Returns 0xFF while the march continues,
 // otherwise the final state (0 hit, 1 out of bounds, 2 step cap); on return
-// r.i is the iteration count the shader reports.
+// r.i is the iteration count the shader reports. kNaN selects the NaN-aware
+// min/argmin (see ray_needs_nan_checks); both variants give identical results
+// on rays where tMax is never NaN.
+template <bool kNaN>
 __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     if (r.i >= kMaxSteps) return 2u;
     // vec3<i32>(floor(p)): one saturating round-down conversion (NaN -> 0).
     const int x = __float2int_rd(r.px), y = __float2int_rd(r.py), z = __float2int_rd(r.pz);
-    const int d = (x ^ r.lx) | (y ^ r.ly) | (z ^ r.lz);
+    const uint32_t d = (uint32_t)((x ^ r.lx) | (y ^ r.ly) | (z ^ r.lz));
     r.lx = x; r.ly = y; r.lz = z;
     int lvl;
-    if (r.np == 3 && (d & ~7) == 0) lvl = 3;
-    else if (r.np >= 2 && (d & ~127) == 0) lvl = 4;
-    else if (r.np >= 1 && (d & ~4095) == 0) lvl = 5;
+    if (r.np == 3 && d < 8u) lvl = 3;
+    else if (r.np >= 2 && d < 128u) lvl = 4;
+    else if (r.np >= 1 && d < 4096u) lvl = 5;
     else lvl = 0;
     uint32_t dist = 1;
     if (lvl == 0) {  // get_vdb_leaf_from_nothing (:398-413): linear scan of the N5 origins
@@ -175,15 +185,18 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
         r.np = 3;
     }
     if (dist == 0u) return 0u;
+    const float apx = fabsf(r.px), apy = fabsf(r.py), apz = fabsf(r.pz);
     // any(4096 < |p|); a NaN coordinate compares false, and fmaxf skips NaN.
-    if (4096.0f < fmaxf(fmaxf(fabsf(r.px), fabsf(r.py)), fabsf(r.pz))) return 1u;
-    // size = f32(dist) * scale[by num_parents] (:105-112)
-    const int sk = r.np == 3 ? 0 : r.np == 2 ? 3 : r.np == 1 ? 7 : 12;
+    if (4096.0f < fmaxf(fmaxf(apx, apy), apz)) return 1u;
+    // size = f32(dist) * scale[by num_parents] (:105-112); log2 scale by np = 12, 7, 3, 0.
+    const int sk = (0x037C >> (r.np << 2)) & 15;
     const float size = __uint2float_rn(dist) * __int_as_float((127 + sk) << 23);
     bool fast;
     const float ys = rcp_size(dist, sk, &fast);
     float qx, qy, qz;
-    if (fast && !(tiny_nonzero(r.px) || tiny_nonzero(r.py) || tiny_nonzero(r.pz))) {
+    // The fast quotient needs every coordinate of magnitude >= 2^-64 (a zero
+    // coordinate also takes the IEEE path here; both give the same floor).
+    if (fast && fminf(fminf(apx, apy), apz) >= 0x1p-64f) {
         qx = div_fast(r.px, size, ys);
         qy = div_fast(r.py, size, ys);
         qz = div_fast(r.pz, size, ys);
@@ -192,23 +205,34 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
         qy = __fdiv_rn(r.py, size);
         qz = __fdiv_rn(r.pz, size);
     }
-    // tMax = idir * (size * step01 - (p - size * floor(p / size)))  (:78-80, :114);
-    // size * step01 is size or +0.
-    const float tx = r.ix * ((r.nx > 0.0f ? size : 0.0f) - (r.px - size * floorf(qx)));
-    const float ty = r.iy * ((r.ny > 0.0f ? size : 0.0f) - (r.py - size * floorf(qy)));
-    const float tz = r.iz * ((r.nz > 0.0f ? size : 0.0f) - (r.pz - size * floorf(qz)));
-    const float t = pmin(pmin(tx, ty), tz);
+    // tMax = idir * (size * step01 - (p - size * floor(p / size)))  (:78-80, :114)
+    const float tx = r.ix * (size * r.ax - (r.px - size * floorf(qx)));
+    const float ty = r.iy * (size * r.ay - (r.py - size * floorf(qy)));
+    const float tz = r.iz * (size * r.az - (r.pz - size * floorf(qz)));
+    float t;
+    bool mx, my, mz;
+    if (kNaN) {
+        t = pmin(pmin(tx, ty), tz);
+        mx = (tx <= ty) && (tx <= tz);
+        my = (ty <= tz) && (ty <= tx);
+        mz = (tz <= tx) && (tz <= ty);
+    } else {
+        // Without NaN: min keeps its first operand on ties, and
+        // (a <= b && a <= c) is a == min(a, b, c) (+0 and -0 compare equal).
+        const float t1 = ty < tx ? ty : tx;
+        t = tz < t1 ? tz : t1;
+        mx = tx == t;
+        my = ty == t;
+        mz = tz == t;
+    }
     r.px = r.px + t * r.dx;
     r.py = r.py + t * r.dy;
     r.pz = r.pz + t * r.dz;
-    const bool mx = (tx <= ty) && (tx <= tz);
-    const bool my = (ty <= tz) && (ty <= tx);
-    const bool mz = (tz <= tx) && (tz <= ty);
-    r.mask = (mx ? 1u : 0u) | (my ? 2u : 0u) | (mz ? 4u : 0u);
-    // p += (4e-4 * step) * f32(mask): the addend is n or n * 0 (a signed zero).
-    r.px = r.px + (mx ? r.nx : r.nx * 0.0f);
-    r.py = r.py + (my ? r.ny : r.ny * 0.0f);
-    r.pz = r.pz + (mz ? r.nz : r.nz * 0.0f);
+    r.mask = (uint32_t)mx | ((uint32_t)my << 1) | ((uint32_t)mz << 2);
+    // p += (4e-4 * step) * f32(mask)  (:122)
+    r.px = r.px + ((r.ax - 0.5f) * 8e-4f) * (mx ? 1.0f : 0.0f);
+    r.py = r.py + ((r.ay - 0.5f) * 8e-4f) * (my ? 1.0f : 0.0f);
+    r.pz = r.pz + ((r.az - 0.5f) * 8e-4f) * (mz ? 1.0f : 0.0f);
     r.i++;
     return 0xFFu;
 }
@@ -231,7 +255,12 @@ __device__ __forceinline__ March hdda(const DevGrid &g, F3 src, F3 dir) {
     Ray r;
     ray_init(r, src, dir);
     uint32_t st;
-    while ((st = ray_step(g, r)) == 0xFFu) {
+    if (ray_needs_nan_checks(dir)) {
+        while ((st = ray_step<true>(g, r)) == 0xFFu) {
+        }
+    } else {
+        while ((st = ray_step<false>(g, r)) == 0xFFu) {
+        }
     }
     March m;
     m.p = f3(r.px, r.py, r.pz);
