@@ -45,6 +45,19 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
+def profiled_traffic(kernel: str, workload: str):
+    """DRAM bytes (read + write) per launch from the committed ncu summary of this kernel and
+    workload (profiles/<kernel>_<workload>_1080p.md, line 'dram_bytes_per_launch: N'), else None."""
+    p = ROOT / "profiles" / f"{kernel}_{workload}_1080p.md"
+    try:
+        for line in p.read_text().splitlines():
+            if line.strip().startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip().split()[0])
+    except OSError:
+        pass
+    return None
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle samples during the timed region."""
 
@@ -189,6 +202,67 @@ def run_reference(args, wl_name):
 # --------------------------------------------------------------------------
 # GPU arm
 # --------------------------------------------------------------------------
+def measure_mixed(ctx, grids, dev, flush, steps, warmup):
+    """BASELINE config 4: 256 requests over the sphere and 2000-sphere grids with resolutions
+    uniform over {256^2, 640x480, 1280x720, 1920x1080, 3840x2160}. Plain = one wx_render
+    launch per request on one stream; batched = one persistent launch over all requests,
+    replayed from a CUDA graph (wx_batch_launch). Both device-timed with CUDA events."""
+    import torch
+
+    from woxel_gb300 import workloads as W
+
+    frames = W.mixed_frames()
+    states = [f.state() for f in frames]
+    outs = [torch.empty(f.width * f.height * 4, dtype=torch.uint8, device=dev) for f in frames]
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    rays = sum(f.rays for f in frames)
+
+    def plain(events=None):
+        for i, (f, st, o) in enumerate(zip(frames, states, outs)):
+            if events is not None:
+                events[i][0].record(stream)
+            ctx.render(grids[f.grid], st, f.width, f.height, o, None, stream=sh)
+            if events is not None:
+                events[i][1].record(stream)
+
+    plan = ctx.batch([(grids[f.grid], st, f.width, f.height, o, None) for f, st, o in zip(frames, states, outs)])
+    for _ in range(warmup):
+        plain()
+        plan.launch(sh)
+    torch.cuda.synchronize()
+    p_ms, b_ms, lat = [], [], []
+    for _ in range(steps):
+        flush.zero_()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in frames]
+        plain(ev)
+        torch.cuda.synchronize()
+        p_ms.append(ev[0][0].elapsed_time(ev[-1][1]))
+        lat.extend(a.elapsed_time(b) for a, b in ev)
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.launch(sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        b_ms.append(e0.elapsed_time(e1))
+    plan.close()
+    lat.sort()
+    pm, bm = statistics.mean(p_ms), statistics.mean(b_ms)
+    return {
+        "workload": "mixed: 256 requests over the sphere + 2000-sphere grids, resolutions "
+                    "256x256..3840x2160 (seeded), mode 3",
+        "rays_per_step": rays,
+        "plain": {"value": rays / (pm / 1e3) / 1e9, "unit": "Grays/s", "ms_per_step": pm,
+                  "request_latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[int(0.99 * (len(lat) - 1))]},
+                  "launches_per_step": len(frames)},
+        "batched": {"value": rays / (bm / 1e3) / 1e9, "unit": "Grays/s", "ms_per_step": bm,
+                    "request_latency_ms": {"p50": bm, "p99": bm, "note": "every request completes with the batch"},
+                    "launches_per_step": 1, "cuda_graph": True},
+        "speedup": pm / bm,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -199,6 +273,7 @@ def main():
     ap.add_argument("--cpu-fraction", type=float, default=1.0 / 8)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the mixed-load batched comparison")
     ap.add_argument("--kernel", default="persistent", choices=["persistent", "pixel"])
     ap.add_argument("--tile-width", type=int, default=None)
     ap.add_argument("--warps-per-block", type=int, default=None)
@@ -313,8 +388,16 @@ def main():
                "h2d_bytes_per_step": 256 * len(frames), "d2h_bytes_per_step": W_ * H_ * 4 * len(frames),
                "ms_per_step": em}
 
+    # BASELINE config 4: batched vs plain on the mixed-resolution load (needs the 2000-sphere grid)
+    batched = None
+    if not args.no_batched and args.workload == "spheres":
+        sphere_grid = ctx.build_grid(W.sphere_topology())
+        batched = measure_mixed(ctx, {"sphere": sphere_grid, "spheres": grid}, dev, flush, args.steps, args.warmup)
+        sphere_grid.release()
+
     # roofline + CPU baseline from the oracle on a sample of the same tiles (rank 0)
     roof, cpu = None, None
+    kernel_name = "k_persistent" if args.kernel == "persistent" else "k_pixel"
     if rank == 0:
         peak, peak_kind = hbm_peak()
         view = topo.view()
@@ -324,8 +407,9 @@ def main():
         bytes_launch = bpr * frames[0].rays
         achieved = bytes_launch / (launch_avg_ms / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "peak_kind": peak_kind, "kernel": "k_render_plain",
-                "algorithmic_bytes_per_ray": bpr, "launch_ms": launch_avg_ms}
+                "traffic": profiled_traffic(kernel_name, args.workload), "peak_kind": peak_kind,
+                "kernel": kernel_name, "algorithmic_bytes_per_ray": bpr,
+                "algorithmic_bytes_per_launch": bytes_launch, "launch_ms": launch_avg_ms}
         if not args.no_cpu:
             cpu = {"value": rays_s / secs / 1e9, "unit": "Grays/s", "cores": nthreads, "kind": "port",
                    "sample": f"{args.cpu_fraction:.4f} of the 8x4 tiles of each of the {len(frames)} frames "
@@ -342,6 +426,7 @@ def main():
                        "render_mode": frames[0].mode, "l2": "flushed between steps (512 MB write)",
                        "parallelism": f"replicas x{world}", "tuning": ctx.tuning},
             "frame_latency_ms": {"p50": p50, "p99": p99},
+            "batched": batched,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "gpu_launches": len(frames) * args.steps,
             "clocks": clk.summary(),

@@ -94,7 +94,7 @@ __global__ void WX_RAY_BOUNDS k_persistent(const Job *__restrict__ jobs, uint32_
         if (kBatched) {
             cur_job = find_job(jobs, njobs, t, cur_job);
             const Job &J = jobs[cur_job];
-            render_pixel(J, t - J.tile_begin, lane);
+            render_pixel(J, t - J.tile_begin + J.tile_off, lane);
         } else {
             render_pixel(job0, t, lane);
         }

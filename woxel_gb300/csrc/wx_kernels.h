@@ -23,7 +23,8 @@ struct Job {
     uint32_t width, height;
     uint32_t tile_w, tile_h;       // pixel tile of one warp (tile_w * tile_h = 32)
     uint32_t tiles_x, tiles;       // tiles per row / per frame over the dispatched region
-    uint32_t tile_begin, pad;      // first global tile id of this job
+    uint32_t tile_begin;           // first global (queue) tile id of this job
+    uint32_t tile_off;             // first frame tile of this job (a job may cover part of a frame)
     uint32_t *rgba;
     wx_hit *hits;
     wx_state_uniform s;
