@@ -263,6 +263,83 @@ def measure_mixed(ctx, grids, dev, flush, steps, warmup):
     }
 
 
+def run_serve(args):
+    """BASELINE config 5: open-loop Poisson arrivals over 8 resident grids (4 sphere-generator
+    grids with distinct seeds, 4 2000-sphere grids with seeds 2..5), resolution mix of config 4,
+    HBM budget 150 GB. Each rate is replayed on the continuous-batching server and on the FIFO
+    single-request server; reports p50/p99 request latency and served Grays/s."""
+    import torch
+
+    import woxel_gb300 as wx
+    from woxel_gb300 import workloads as W
+
+    torch.cuda.set_device(0)
+    ctx = wx.Context(0)
+    t0 = time.perf_counter()
+    grids, kinds = [], []
+    for s in range(4):
+        grids.append(ctx.build_grid(W.sphere_topology(s)))
+        kinds.append("sphere")
+    for s in range(2, 6):
+        grids.append(ctx.build_grid(W.spheres_topology(s)))
+        kinds.append("spheres")
+    grid_bytes = sum(g.info["device_bytes"] for g in grids)
+    log(f"[serve] 8 grids, {grid_bytes / 1e9:.2f} GB of node pools, built in {time.perf_counter() - t0:.1f}s")
+    rates = [float(r) for r in args.serve_rates.split(",")]
+    budget = 150 * 10**9
+
+    def trace(rate, seed):
+        rng = np.random.default_rng(seed)
+        n = max(1, int(rng.poisson(rate * args.serve_duration)))
+        arr = np.sort(rng.uniform(0, args.serve_duration, size=n))
+        reqs, rays = [], 0
+        for i in range(n):
+            gid = int(rng.integers(0, len(grids)))
+            w, h = W.RESOLUTIONS[int(rng.integers(0, len(W.RESOLUTIONS)))]
+            radius = 200.0 if kinds[gid] == "sphere" else 3000.0
+            eye = wx.orbit_eyes(1, radius, int(rng.integers(0, 2**62)))[0]
+            st = wx.state_build(eye=tuple(float(x) for x in eye), target=(0, 0, 0), aspect=w / h, fovy=60.0,
+                                width=float(w), mode=3)
+            reqs.append(wx.Server.request(gid, st, w, h, user=i))
+            rays += (w // 8) * 8 * (h // 4) * 4
+        return reqs, list(arr), rays
+
+    out = []
+    for mode in ("batched", "fifo"):
+        srv = wx.Server(ctx, budget_bytes=budget, max_inflight=2, slice_tiles=args.serve_slice, fifo=(mode == "fifo"))
+        for g in grids:
+            srv.add_grid(g)
+        # warm-up: a few requests
+        wreqs, warr, _ = trace(50.0, 1)
+        srv.replay(wreqs[:8], [0.0] * min(8, len(wreqs)), release=True)
+        for k, rate in enumerate(rates):
+            reqs, arr, rays = trace(rate, 1000 + k)
+            t1 = time.perf_counter()
+            res = srv.replay(reqs, arr, release=True, timeout_s=args.serve_timeout)
+            wall = time.perf_counter() - t1
+            lat = np.array([r.t_done - r.t_submit for r in res]) * 1e3
+            first = min(r.t_submit for r in res)
+            last = max(r.t_done for r in res)
+            out.append({"mode": mode, "rate_req_s": rate, "requests": len(reqs), "offered_grays_per_s": rays / args.serve_duration / 1e9,
+                        "served_grays_per_s": rays / (last - first) / 1e9, "latency_ms_p50": float(np.percentile(lat, 50)),
+                        "latency_ms_p99": float(np.percentile(lat, 99)), "wall_s": wall})
+            log(f"[serve] {mode} {rate:.0f} req/s: {out[-1]}")
+        stats = srv.stats
+        out[-1]["launches_total"] = stats["launches"]
+        srv.close()
+    best = max((o for o in out if o["mode"] == "batched"), key=lambda o: o["served_grays_per_s"])
+    fifo_best = max((o for o in out if o["mode"] == "fifo"), key=lambda o: o["served_grays_per_s"])
+    print(json.dumps({
+        "metric": "served_primary_ray_grays_per_s", "value": best["served_grays_per_s"], "unit": "Grays/s",
+        "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "serving: Poisson arrivals over 8 resident grids (4 sphere, 4 2000-sphere), "
+                               "resolutions 256x256..3840x2160, mode 3", "budget_bytes": budget,
+                   "grid_bytes": grid_bytes, "duration_s_per_rate": args.serve_duration,
+                   "slice_tiles": args.serve_slice, "max_inflight": 2},
+        "fifo_value": fifo_best["served_grays_per_s"], "sweep": out,
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -274,6 +351,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the mixed-load batched comparison")
+    ap.add_argument("--serve", action="store_true", help="run the serving sweep (config 5) instead")
+    ap.add_argument("--serve-rates", default="100,200,500,1000,2000,5000")
+    ap.add_argument("--serve-duration", type=float, default=5.0, help="seconds of arrivals per rate")
+    ap.add_argument("--serve-slice", type=int, default=65536, help="tiles per launch")
+    ap.add_argument("--serve-timeout", type=float, default=300.0)
     ap.add_argument("--kernel", default="persistent", choices=["persistent", "pixel"])
     ap.add_argument("--tile-width", type=int, default=None)
     ap.add_argument("--warps-per-block", type=int, default=None)
@@ -281,6 +363,9 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args, args.workload)
+        return
+    if args.serve:
+        run_serve(args)
         return
 
     import torch

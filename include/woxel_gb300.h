@@ -193,6 +193,75 @@ int wx_batch_destroy(wx_batch *batch);
 #define WX_NOALLOC_SCRATCH_BYTES 88320 /* 256 + 256 frames x 344-byte table entries */
 int wx_render_batch_noalloc(const wx_frame *frames, uint32_t n, void *stream);
 
+/* ---- serving: continuous batching of render requests (no counterpart in the
+ * reference, whose render loop draws one frame per window event,
+ * src/runtime.rs:97-109). Requests are admitted in arrival order while their
+ * output buffers fit the HBM budget, then rendered in time-sliced batches
+ * (at most slice_tiles 8x4 tiles per launch, a large request spanning several
+ * slices) with up to max_inflight launches in flight, so requests that arrive
+ * while others are on the GPU join the next slice. Grids stay resident. ---- */
+typedef struct wx_server wx_server;
+
+#define WX_SERVE_FIFO 1u /* baseline: one whole request per launch, one launch in flight */
+
+typedef struct wx_server_config {
+    uint64_t budget_bytes;  /* HBM budget: resident grids + the output arena */
+    uint32_t max_inflight;  /* launches in flight, 1..8 (default 2) */
+    uint32_t slice_tiles;   /* tiles per launch; 0 = 65536 (one 1080p frame) */
+    uint32_t max_frames;    /* request pieces per launch, 1..1024 (default 256) */
+    uint32_t flags;         /* WX_SERVE_FIFO */
+} wx_server_config;
+
+typedef struct wx_request {
+    uint32_t grid_id;       /* from wx_server_add_grid */
+    uint32_t want_hits;     /* nonzero: also produce wx_hit records */
+    uint32_t width, height;
+    wx_state_uniform state;
+    uint64_t user;          /* returned unchanged in the result */
+} wx_request;
+
+typedef struct wx_result {
+    uint64_t ticket, user;
+    int32_t status;         /* WX_OK, or WX_ERR_CANCELLED */
+    uint32_t width, height;
+    const uint8_t *rgba8;   /* device memory in the server's arena, valid until wx_server_release */
+    const wx_hit *hits;     /* NULL unless requested */
+    double t_submit, t_admit, t_done; /* seconds on the server's steady clock */
+} wx_result;
+
+typedef struct wx_server_stats {
+    uint64_t submitted, completed, cancelled, launches;
+    uint64_t rays_done;        /* dispatched pixels of completed requests */
+    uint64_t arena_bytes, arena_in_use, arena_peak;
+    uint64_t pending, active;
+} wx_server_stats;
+
+/* Creates the scheduler and allocates the output arena (budget minus the
+ * grids added later is checked at admission). */
+int wx_server_create(wx_ctx *ctx, const wx_server_config *cfg, wx_server **out);
+/* Registers a resident grid; its device bytes count against the budget. */
+int wx_server_add_grid(wx_server *srv, const wx_grid *grid, uint32_t *grid_id);
+/* Queues a request (never blocks on the GPU). WX_ERR_BUDGET if it could never fit. */
+int wx_server_submit(wx_server *srv, const wx_request *req, uint64_t *ticket);
+/* Cancels a request that has not been admitted yet (its result reports WX_ERR_CANCELLED). */
+int wx_server_cancel(wx_server *srv, uint64_t ticket);
+/* Moves up to max finished results into out; waits up to wait_ms for the first. */
+int wx_server_poll(wx_server *srv, wx_result *out, uint32_t max, uint32_t *n, int wait_ms);
+/* Copies a polled result's rgba8 (width*height*4 bytes) and, if requested,
+ * hits (width*height records) into host memory; either pointer may be NULL. */
+int wx_server_copy_result(wx_server *srv, uint64_t ticket, uint8_t *rgba8_host, wx_hit *hits_host);
+/* Returns a finished request's buffers to the arena. */
+int wx_server_release(wx_server *srv, uint64_t ticket);
+int wx_server_get_stats(wx_server *srv, wx_server_stats *out);
+/* Open-loop replay: submits reqs[i] at arrival_s[i] seconds after the call,
+ * collects every result into results[i] (in request order), releasing buffers
+ * as results arrive when release != 0. Returns when all have finished or
+ * timeout_s elapses (WX_ERR_TIMEOUT). */
+int wx_server_replay(wx_server *srv, const wx_request *reqs, const double *arrival_s, uint32_t n,
+                     wx_result *results, int release, double timeout_s);
+/* Stops the scheduler (waits for in-flight launches) and frees the arena. */
+int wx_server_destroy(wx_server *srv);
+
 /* Exhaustive GPU check of the kernels' fast floor(p / size) path against IEEE
  * division: every odd divisor m < max_m (<= 4096) and every significand of
  * [1,2) and [-2,-1). out = {mismatches, first bad m, its x bits}. */

@@ -335,3 +335,88 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+# --------------------------------------------------------------------------
+# Serving: continuous batching of render requests (wx_server_*)
+# --------------------------------------------------------------------------
+from ._ffi import wx_request, wx_result, wx_server_config, wx_server_stats  # noqa: E402
+
+SERVE_FIFO = 1
+
+
+class Server:
+    """Continuous-batching render server over resident grids (see include/woxel_gb300.h).
+
+    Results live in the server's device arena until release(ticket)."""
+
+    def __init__(self, ctx: Context, budget_bytes: int, max_inflight: int = 2, slice_tiles: int = 0,
+                 max_frames: int = 0, fifo: bool = False):
+        cfg = wx_server_config(budget_bytes, max_inflight, slice_tiles, max_frames, SERVE_FIFO if fifo else 0)
+        out = C.c_void_p()
+        check(lib().wx_server_create(ctx._h, C.byref(cfg), C.byref(out)))
+        self.ctx = ctx
+        self._h = out
+        self._grids = []
+
+    def add_grid(self, grid: Grid) -> int:
+        gid = C.c_uint32()
+        check(lib().wx_server_add_grid(self._h, grid._h, C.byref(gid)))
+        self._grids.append(grid)
+        return gid.value
+
+    @staticmethod
+    def request(grid_id: int, state: wx_state_uniform, width: int, height: int, hits: bool = False,
+                user: int = 0) -> wx_request:
+        return wx_request(grid_id, 1 if hits else 0, width, height, state, user)
+
+    def submit(self, req: wx_request) -> int:
+        t = C.c_uint64()
+        check(lib().wx_server_submit(self._h, C.byref(req), C.byref(t)))
+        return t.value
+
+    def cancel(self, ticket: int) -> None:
+        check(lib().wx_server_cancel(self._h, ticket))
+
+    def poll(self, max_results: int = 64, wait_ms: int = 0) -> list:
+        out = (wx_result * max_results)()
+        n = C.c_uint32()
+        check(lib().wx_server_poll(self._h, out, max_results, C.byref(n), wait_ms))
+        return [out[i] for i in range(n.value)]
+
+    def release(self, ticket: int) -> None:
+        check(lib().wx_server_release(self._h, ticket))
+
+    def fetch(self, result: wx_result, hits: bool = False) -> tuple:
+        """Host copies of a polled result: rgba[h, w, 4] and (optionally) hits[h, w]."""
+        w, h = result.width, result.height
+        rgba = np.zeros((h, w, 4), np.uint8)
+        hb = np.zeros((h, w), HIT_DTYPE) if hits else None
+        check(lib().wx_server_copy_result(self._h, result.ticket, rgba.ctypes.data,
+                                          None if hb is None else hb.ctypes.data))
+        return rgba, hb
+
+    @property
+    def stats(self) -> dict:
+        s = wx_server_stats()
+        check(lib().wx_server_get_stats(self._h, C.byref(s)))
+        return {k: int(getattr(s, k)) for k, _ in wx_server_stats._fields_}
+
+    def replay(self, reqs: Sequence, arrivals: Sequence, release: bool = True, timeout_s: float = 600.0) -> list:
+        n = len(reqs)
+        ra = (wx_request * n)(*reqs)
+        ta = (C.c_double * n)(*arrivals)
+        res = (wx_result * n)()
+        check(lib().wx_server_replay(self._h, ra, ta, n, res, 1 if release else 0, timeout_s))
+        return [res[i] for i in range(n)]
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            lib().wx_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -45,6 +45,29 @@ class wx_frame(C.Structure):
                 ("rgba8", C.c_void_p), ("hits", C.c_void_p)]
 
 
+class wx_server_config(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("max_inflight", C.c_uint32), ("slice_tiles", C.c_uint32),
+                ("max_frames", C.c_uint32), ("flags", C.c_uint32)]
+
+
+class wx_request(C.Structure):
+    _fields_ = [("grid_id", C.c_uint32), ("want_hits", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("state", wx_state_uniform), ("user", C.c_uint64)]
+
+
+class wx_result(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("user", C.c_uint64), ("status", C.c_int32), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("rgba8", C.c_void_p), ("hits", C.c_void_p), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_done", C.c_double)]
+
+
+class wx_server_stats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("cancelled", C.c_uint64),
+                ("launches", C.c_uint64), ("rays_done", C.c_uint64), ("arena_bytes", C.c_uint64),
+                ("arena_in_use", C.c_uint64), ("arena_peak", C.c_uint64), ("pending", C.c_uint64),
+                ("active", C.c_uint64)]
+
+
 assert C.sizeof(wx_state_uniform) == 256
 assert C.sizeof(wx_hit) == 32
 
@@ -72,6 +95,17 @@ SIGNATURES = {
     "wx_batch_info": (INT, [P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U64)]),
     "wx_batch_destroy": (INT, [P]),
     "wx_render_batch_noalloc": (INT, [C.POINTER(wx_frame), U32, P]),
+    "wx_server_create": (INT, [P, C.POINTER(wx_server_config), C.POINTER(P)]),
+    "wx_server_add_grid": (INT, [P, P, C.POINTER(U32)]),
+    "wx_server_submit": (INT, [P, C.POINTER(wx_request), C.POINTER(U64)]),
+    "wx_server_cancel": (INT, [P, U64]),
+    "wx_server_poll": (INT, [P, C.POINTER(wx_result), U32, C.POINTER(U32), INT]),
+    "wx_server_release": (INT, [P, U64]),
+    "wx_server_copy_result": (INT, [P, U64, P, P]),
+    "wx_server_get_stats": (INT, [P, C.POINTER(wx_server_stats)]),
+    "wx_server_replay": (INT, [P, C.POINTER(wx_request), C.POINTER(C.c_double), U32, C.POINTER(wx_result), INT,
+                               C.c_double]),
+    "wx_server_destroy": (INT, [P]),
     "wx_check_division": (INT, [P, U32, C.POINTER(U64)]),
     "wx_state_build": (INT, [P, P, P, F32, F32, F32, U32, P, P, P, F32, C.POINTER(wx_state_uniform)]),
     "wx_sun_default": (None, [P, P, P]),

@@ -160,6 +160,11 @@ wxk::Job make_job(const wx_grid *grid, const wx_state_uniform &s, uint32_t width
 
 }  // namespace
 
+void wxk::ctx_device_info(const wx_ctx *ctx, int *device, int *num_sms) {
+    *device = ctx->device;
+    *num_sms = ctx->num_sms;
+}
+
 bool wxk::grid_device_view(const wx_grid *grid, wxk::DevGrid *out, int *device) {
     if (!grid) return false;
     *out = grid->g;

@@ -45,6 +45,8 @@ cudaError_t launch_batched(const Job *jobs_dev, uint32_t njobs, uint32_t total_t
                            const Tuning &t, int num_sms, cudaStream_t st);
 // Device pools and device of a grid handle (defined in api.cpp); false for NULL.
 bool grid_device_view(const wx_grid *grid, DevGrid *out, int *device);
+// Device index and SM count of a context (defined in api.cpp).
+void ctx_device_info(const wx_ctx *ctx, int *device, int *num_sms);
 
 // Exhaustive check of the fast floor-division path against IEEE division:
 // every odd m < max_m and every significand of [1,2) and [-2,-1).
