@@ -351,6 +351,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the mixed-load batched comparison")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the default launch shape instead of autotuning on 4 frames")
     ap.add_argument("--serve", action="store_true", help="run the serving sweep (config 5) instead")
     ap.add_argument("--serve-rates", default="100,200,500,1000,2000,5000")
     ap.add_argument("--serve-duration", type=float, default=5.0, help="seconds of arrivals per rate")
@@ -416,6 +418,13 @@ def main():
             if events is not None:
                 events[i][1].record(stream)
 
+    tuned = None
+    if args.autotune and args.kernel == "persistent" and args.tile_width is None and args.warps_per_block is None:
+        t0 = time.perf_counter()
+        tuned = ctx.autotune([(grid, st, W_, H_, o, None) for st, o in list(zip(states, outs))[:4]], reps=2)
+        tuned["seconds"] = time.perf_counter() - t0
+        tuned["table"] = [[c["kernel"], c["tile_width"], c["warps_per_block"], round(ms, 4)] for c, ms in tuned["table"]]
+        log(f"[bench] autotune -> {tuned['best']} in {tuned['seconds']:.1f}s")
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -509,7 +518,9 @@ def main():
             "config": {"workload": f"{args.workload}: {len(frames)} x {W_}x{H_} frames, plain per-frame launches",
                        "grid": {k: info[k] for k in ("n5", "n4", "n3", "active_voxels", "device_bytes")},
                        "render_mode": frames[0].mode, "l2": "flushed between steps (512 MB write)",
-                       "parallelism": f"replicas x{world}", "tuning": ctx.tuning},
+                       "parallelism": f"replicas x{world}", "tuning": ctx.tuning,
+                       "autotune": tuned and {"table [kernel, tile_w, warps/block, ms for 4 frames]": tuned["table"],
+                                              "seconds": tuned["seconds"]}},
             "frame_latency_ms": {"p50": p50, "p99": p99},
             "batched": batched,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,

@@ -153,6 +153,14 @@ int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, u
  * notes the workgroup choice as a TODO) ---- */
 int wx_ctx_set_tuning(wx_ctx *ctx, const wx_tuning *tuning);
 int wx_ctx_get_tuning(const wx_ctx *ctx, wx_tuning *tuning);
+/* Autotuner: renders `frames` (device outputs, as for wx_render_batch) once per
+ * frame with each candidate tuning, reps times after one warm-up pass, timing
+ * with CUDA events, and installs the fastest on the context. candidates NULL
+ * (ncand ignored) uses the built-in set: both kernels x tile widths {4, 8, 16}
+ * x {2, 4, 8} warps per block. times_ms (ncand or 18 entries, may be NULL)
+ * receives each candidate's mean time for all frames. */
+int wx_autotune(wx_ctx *ctx, const wx_frame *frames, uint32_t n, const wx_tuning *candidates, uint32_t ncand,
+                uint32_t reps, wx_tuning *best, double *times_ms);
 
 /* ---- batched rendering: many cameras over several resident grids in one
  * persistent launch drawing 8x4 ray tiles from a global queue. Per frame the
@@ -299,6 +307,18 @@ int wx_topology_sdf(wx_topology *topo, int nthreads);
  * Pass NULL atlases to query sides. Leaf value texels are written as value_texel. */
 int wx_topology_atlas(const wx_topology *topo, uint32_t side[3], uint32_t *a5, uint32_t *a4,
                       uint32_t *a3, uint32_t value_texel);
+
+/* ---- OpenVDB files: VdbReader::new + read_vdb345_grid (src/vdb/read.rs:62-349) ----
+ * Reads the tree topology of one grid (grid_name NULL = the first) of an
+ * uncompressed or active-mask-compressed file (the reference's assets use
+ * flag 2: active mask, half-float values). Leaf values are not read: the march
+ * only uses the value masks. Blosc/zip files give WX_ERR_UNSUPPORTED. */
+typedef struct wx_vdb_info {
+    uint32_t file_version, compression, half_float, reserved;
+    int64_t file_voxel_count; /* grid metadata "file_voxel_count", -1 if absent */
+    char grid_name[64];
+} wx_vdb_info;
+int wx_vdb_read_topology(const char *path, const char *grid_name, wx_topology **out, wx_vdb_info *info);
 
 /* ---- synthetic grids (seeded; f32 narrow-band level sets use value = signed distance) ---- */
 /* Voxels with |(|ijk - c| - r)| < band are active. */

@@ -87,6 +87,22 @@ def test_batch_graph_plan_replays(cuda_ctx, scene):
     plan.close()
 
 
+def test_autotune_installs_a_candidate_and_keeps_results(cuda_ctx, scene):
+    views, grids, frames = scene
+    before = cuda_ctx.tuning
+    big = [f for f in frames if f[2] * f[3] >= 96 * 96]
+    outs = alloc(big)
+    res = cuda_ctx.autotune([(grids[gi], st, w, h, o[0], None) for (gi, st, w, h), o in zip(big, outs)],
+                            candidates=[dict(kernel=0, tile_width=8), dict(kernel=1, tile_width=16, warps_per_block=2),
+                                        dict(kernel=0, tile_width=4, warps_per_block=8)], reps=1)
+    assert res["best"] == cuda_ctx.tuning and len(res["table"]) == 3 and all(ms > 0 for _, ms in res["table"])
+    gi, st, w, h = big[0]
+    rg, hg = gpu_render(cuda_ctx, grids[gi], st, w, h)
+    ro, ho = oracle_render(views[gi], st, w, h)
+    compare(rg, hg, ro, ho, label="after autotune")
+    cuda_ctx.set_tuning(**before)
+
+
 def test_batch_rejects_host_outputs(cuda_ctx, scene):
     _, grids, frames = scene
     gi, st, w, h = frames[0]

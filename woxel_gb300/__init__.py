@@ -71,6 +71,19 @@ class Topology:
         return cls._make(lib().wx_gen_noise_leaves, lo, extent, occupancy, p_voxel, seed, nthreads)
 
     @classmethod
+    def read_vdb(cls, path, grid_name: Optional[str] = None) -> tuple:
+        """Topology of one grid of an OpenVDB file, and the file's info (version, voxel-count metadata)."""
+        from ._ffi import wx_vdb_info
+
+        out, info = C.c_void_p(), wx_vdb_info()
+        check(lib().wx_vdb_read_topology(str(path).encode(), grid_name.encode() if grid_name else None,
+                                         C.byref(out), C.byref(info)))
+        meta = {"file_version": info.file_version, "compression": info.compression,
+                "half_float": bool(info.half_float), "file_voxel_count": info.file_voxel_count,
+                "grid_name": info.grid_name.decode()}
+        return Topology(out.value), meta
+
+    @classmethod
     def from_voxels(cls, ijk) -> "Topology":
         a = np.ascontiguousarray(ijk, dtype=np.int32).reshape(-1, 3)
         return cls._make(lib().wx_topology_from_voxels, a.ctypes.data, a.shape[0])
@@ -265,6 +278,22 @@ class Context:
         cur.update(kw)
         t = wx_tuning(**cur)
         check(lib().wx_ctx_set_tuning(self._h, C.byref(t)), self._h)
+
+    def autotune(self, frames: Sequence, candidates: Optional[Sequence[dict]] = None, reps: int = 3) -> dict:
+        """Time candidate launch shapes on `frames` ((grid, state, w, h, rgba_dev, hits_dev) tuples) and
+        install the fastest. Returns {"best": tuning, "table": [(tuning, ms), ...]}."""
+        arr = self._frames(frames)
+        if candidates is None:
+            cands = [dict(kernel=k, warps_per_block=w, blocks_per_sm=0, tile_width=t)
+                     for k in (0, 1) for t in (4, 8, 16) for w in (2, 4, 8)]
+        else:
+            cands = [dict(self.tuning, **c) for c in candidates]
+        carr = (wx_tuning * len(cands))(*[wx_tuning(**c) for c in cands])
+        times = (C.c_double * len(cands))()
+        best = wx_tuning()
+        check(lib().wx_autotune(self._h, arr, len(frames), carr, len(cands), reps, C.byref(best), times), self._h)
+        return {"best": {k: int(getattr(best, k)) for k, _ in wx_tuning._fields_},
+                "table": [(c, float(times[i])) for i, c in enumerate(cands)]}
 
     def check_division(self, max_m: int = 4096) -> tuple:
         out = (C.c_uint64 * 3)()

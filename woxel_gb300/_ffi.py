@@ -68,6 +68,11 @@ class wx_server_stats(C.Structure):
                 ("active", C.c_uint64)]
 
 
+class wx_vdb_info(C.Structure):
+    _fields_ = [("file_version", C.c_uint32), ("compression", C.c_uint32), ("half_float", C.c_uint32),
+                ("reserved", C.c_uint32), ("file_voxel_count", C.c_int64), ("grid_name", C.c_char * 64)]
+
+
 assert C.sizeof(wx_state_uniform) == 256
 assert C.sizeof(wx_hit) == 32
 
@@ -107,6 +112,8 @@ SIGNATURES = {
                                C.c_double]),
     "wx_server_destroy": (INT, [P]),
     "wx_check_division": (INT, [P, U32, C.POINTER(U64)]),
+    "wx_autotune": (INT, [P, C.POINTER(wx_frame), U32, C.POINTER(wx_tuning), U32, U32, C.POINTER(wx_tuning),
+                          C.POINTER(C.c_double)]),
     "wx_state_build": (INT, [P, P, P, F32, F32, F32, U32, P, P, P, F32, C.POINTER(wx_state_uniform)]),
     "wx_sun_default": (None, [P, P, P]),
     "wx_topology_from_masks": (INT, [P, P, U64, P, P, U64, P, U64, P, U32, C.POINTER(P)]),
@@ -122,6 +129,7 @@ SIGNATURES = {
     "wx_gen_spheres": (INT, [U32, F32, F32, F32, F32, F32, U64, C.POINTER(P)]),
     "wx_gen_noise_leaves": (INT, [I32, U32, C.c_double, C.c_double, U64, INT, C.POINTER(P)]),
     "wx_orbit_eyes": (INT, [U32, F32, U64, P]),
+    "wx_vdb_read_topology": (INT, [C.c_char_p, C.c_char_p, C.POINTER(P), C.POINTER(wx_vdb_info)]),
 }
 
 _lib = None

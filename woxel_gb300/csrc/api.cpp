@@ -257,6 +257,64 @@ int wx_ctx_get_tuning(const wx_ctx *ctx, wx_tuning *t) {
     return WX_OK;
 }
 
+int wx_autotune(wx_ctx *ctx, const wx_frame *frames, uint32_t n, const wx_tuning *candidates, uint32_t ncand,
+                uint32_t reps, wx_tuning *best, double *times_ms) {
+    if (!ctx || !frames || n == 0 || !best) return fail(ctx, WX_ERR_INVALID, "wx_autotune: null argument");
+    WX_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<wx_tuning> cand;
+    if (candidates) {
+        cand.assign(candidates, candidates + ncand);
+    } else {
+        for (int kernel : {0, 1})
+            for (int tw : {4, 8, 16})
+                for (int wpb : {2, 4, 8}) cand.push_back(wx_tuning{kernel, wpb, 0, tw});
+    }
+    if (cand.empty()) return fail(ctx, WX_ERR_INVALID, "wx_autotune: no candidates");
+    for (uint32_t i = 0; i < n; i++)
+        if (!frames[i].grid || !frames[i].rgba8 || !device_accessible(frames[i].rgba8))
+            return fail(ctx, WX_ERR_INVALID, "wx_autotune: frames need a grid and device rgba8");
+    const wxk::Tuning saved = ctx->tuning;
+    cudaEvent_t e0, e1;
+    WX_CUDA(ctx, cudaEventCreate(&e0));
+    WX_CUDA(ctx, cudaEventCreate(&e1));
+    cudaStream_t st;
+    WX_CUDA(ctx, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    double best_ms = 1e300;
+    size_t best_i = 0;
+    int rc = WX_OK;
+    for (size_t c = 0; c < cand.size() && rc == WX_OK; c++) {
+        rc = wx_ctx_set_tuning(ctx, &cand[c]);
+        if (rc != WX_OK) break;
+        double total = 0;
+        for (uint32_t rep = 0; rep <= reps && rc == WX_OK; rep++) {  // pass 0 warms up
+            cudaEventRecord(e0, st);
+            for (uint32_t i = 0; i < n && rc == WX_OK; i++)
+                rc = wx_render(ctx, frames[i].grid, &frames[i].state, frames[i].width, frames[i].height,
+                               frames[i].rgba8, frames[i].hits, st);
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0) total += ms;
+        }
+        const double mean = total / (reps ? reps : 1);
+        if (times_ms) times_ms[c] = mean;
+        if (rc == WX_OK && mean < best_ms) {
+            best_ms = mean;
+            best_i = c;
+        }
+    }
+    cudaStreamDestroy(st);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != WX_OK) {
+        ctx->tuning = saved;
+        return rc;
+    }
+    *best = cand[best_i];
+    return wx_ctx_set_tuning(ctx, best);
+}
+
 int wx_check_division(wx_ctx *ctx, uint32_t max_m, uint64_t out[3]) {
     if (!ctx || !out) return fail(ctx, WX_ERR_INVALID, "wx_check_division: null argument");
     WX_CUDA(ctx, cudaSetDevice(ctx->device));

@@ -1,0 +1,281 @@
+// vdbio.cpp — topology reader for OpenVDB files holding VDB345 grids.
+//
+// Follows woxel's VdbReader (src/vdb/read.rs): archive header (:62-121),
+// grid descriptors (:166-211), per-grid metadata and transform (:123-164,
+// :213-268), and the tree topology (:270-349) with its compressed node
+// headers (:351-488). Only the topology is needed by the raycast pass: leaf
+// values never enter the march (a voxel hits by its value-mask bit), and the
+// reference sets LeafData::Value exactly where the topology's leaf mask is set
+// (read.rs:610-620). The tree-data section is therefore not parsed.
+// Blosc- or zip-compressed node headers are rejected (WX_ERR_UNSUPPORTED).
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "wx_common.h"
+
+namespace {
+
+constexpr uint32_t kMinVersion = 218;            // OPENVDB_FILE_VERSION_BOOST_UUID
+constexpr uint32_t kSelectiveCompression = 220;  // read.rs:27
+constexpr uint32_t kNodeMaskCompression = 222;   // read.rs:28
+constexpr uint32_t kPerGridCompression = 223;    // read.rs:26
+constexpr uint32_t kZip = 0x1, kActiveMask = 0x2, kBlosc = 0x4;
+
+struct Reader {
+    FILE *f = nullptr;
+    std::string err;
+    bool ok = true;
+    bool bytes(void *dst, size_t n) {
+        if (!ok) return false;
+        if (n && fread(dst, 1, n, f) != n) {
+            ok = false;
+            err = "unexpected end of file";
+        }
+        return ok;
+    }
+    template <class T>
+    T get() {
+        T v{};
+        bytes(&v, sizeof v);
+        return v;
+    }
+    std::string str(size_t n) {
+        std::string s(n, '\0');
+        bytes(&s[0], n);
+        return s;
+    }
+    std::string lstr() { return str(get<uint32_t>()); }
+    bool skip(long n) {
+        if (ok && fseek(f, n, SEEK_CUR) != 0) {
+            ok = false;
+            err = "seek failed";
+        }
+        return ok;
+    }
+    bool seek(uint64_t pos) {
+        if (ok && fseek(f, (long)pos, SEEK_SET) != 0) {
+            ok = false;
+            err = "seek failed";
+        }
+        return ok;
+    }
+    bool fail(const std::string &m) {
+        if (ok) err = m;
+        ok = false;
+        return false;
+    }
+};
+
+struct Meta {
+    int64_t voxel_count = -1;
+    bool half = false;
+};
+
+// read_metadata (read.rs:213-268): the reference reads the typed value by type
+// (not by the stored length) for string/bool/int32/int64/float/vec3i.
+Meta read_metadata(Reader &r) {
+    Meta m;
+    const uint32_t n = r.get<uint32_t>();
+    for (uint32_t i = 0; i < n && r.ok; i++) {
+        const std::string name = r.lstr(), type = r.lstr();
+        const uint32_t len = r.get<uint32_t>();
+        if (type == "string") r.skip(len);
+        else if (type == "bool") {
+            const uint8_t v = r.get<uint8_t>();
+            if (name == "is_saved_as_half_float") m.half = v == 1;
+        } else if (type == "int32") r.get<int32_t>();
+        else if (type == "int64") {
+            const int64_t v = r.get<int64_t>();
+            if (name == "file_voxel_count") m.voxel_count = v;
+        } else if (type == "float") r.get<float>();
+        else if (type == "vec3i") r.skip(12);
+        else r.skip(len);
+    }
+    return m;
+}
+
+struct Grid {
+    std::string name, type;
+    uint64_t grid_pos = 0, block_pos = 0, end_pos = 0;
+    uint32_t compression = 0;
+    Meta meta;
+};
+
+// read_compressed (read.rs:378-488) for a node header whose values are not
+// kept: consumes exactly the bytes the reference reads.
+bool skip_compressed(Reader &r, uint32_t version, const Grid &g, size_t size, const std::vector<uint64_t> &vmask) {
+    uint8_t meta = 6;  // NoMaskAndAllVals
+    if (version >= kNodeMaskCompression) meta = r.get<uint8_t>();
+    if (meta > 6) return r.fail("invalid node metadata");
+    if (meta == 2 || meta == 4) r.skip(4);  // one inactive value (ValueType = u32 in the reference)
+    else if (meta == 5) r.skip(8);          // two inactive values
+    if (meta == 3 || meta == 4 || meta == 5) r.skip((long)(size / 64) * 8);  // selection mask
+    size_t count = size;
+    if ((g.compression & kActiveMask) && meta != 6 && version >= kNodeMaskCompression) {
+        count = 0;
+        for (uint64_t w : vmask) count += (size_t)__builtin_popcountll(w);
+    }
+    if (g.compression & (kBlosc | kZip)) return r.fail("blosc/zip-compressed grids are not supported");
+    r.skip((long)(count * (g.meta.half ? 2 : 4)));
+    return r.ok;
+}
+
+}  // namespace
+
+extern "C" int wx_vdb_read_topology(const char *path, const char *grid_name, wx_topology **out, wx_vdb_info *info) {
+    if (!path || !out) {
+        wx::set_thread_error("wx_vdb_read_topology: null argument");
+        return WX_ERR_INVALID;
+    }
+    Reader r;
+    r.f = fopen(path, "rb");
+    if (!r.f) {
+        wx::set_thread_error(std::string("wx_vdb_read_topology: cannot open ") + path);
+        return WX_ERR_INVALID;
+    }
+    struct Closer {
+        FILE *f;
+        ~Closer() { fclose(f); }
+    } closer{r.f};
+    auto bad = [&](int code, const std::string &m) {
+        wx::set_thread_error("wx_vdb_read_topology: " + m);
+        return code;
+    };
+    // Archive header (read.rs:62-121).
+    if (r.get<uint64_t>() != 0x56444220ull) return bad(WX_ERR_INVALID, "magic bytes mismatched");
+    const uint32_t version = r.get<uint32_t>();
+    if (version < kMinVersion) return bad(WX_ERR_UNSUPPORTED, "unsupported file version");
+    r.get<uint32_t>();  // library major
+    r.get<uint32_t>();  // library minor
+    const bool has_offsets = r.get<uint8_t>() != 0;
+    uint32_t compression = version < kPerGridCompression ? (kZip | kActiveMask) : (kBlosc | kActiveMask);
+    if (version >= kSelectiveCompression && version < kNodeMaskCompression)
+        compression = r.get<uint8_t>() == 1 ? kZip : 0;
+    r.skip(36);  // uuid
+    read_metadata(r);
+    const uint32_t ngrids = r.get<uint32_t>();
+    if (!r.ok) return bad(WX_ERR_INVALID, r.err);
+    if (!has_offsets) return bad(WX_ERR_UNSUPPORTED, "file without grid offsets");
+    // Grid descriptors (read.rs:166-211).
+    std::vector<Grid> grids;
+    for (uint32_t i = 0; i < ngrids && r.ok; i++) {
+        Grid g;
+        g.name = r.lstr();
+        g.type = r.lstr();
+        r.lstr();  // instance parent
+        g.grid_pos = r.get<uint64_t>();
+        g.block_pos = r.get<uint64_t>();
+        g.end_pos = r.get<uint64_t>();
+        g.compression = compression;
+        if (version >= kNodeMaskCompression) g.compression = r.get<uint32_t>();
+        g.meta = read_metadata(r);
+        grids.push_back(g);
+        r.seek(g.end_pos);
+    }
+    if (!r.ok) return bad(WX_ERR_INVALID, r.err);
+    const Grid *gp = nullptr;
+    for (const Grid &g : grids)
+        if (!grid_name || g.name == grid_name) {
+            gp = &g;
+            break;
+        }
+    if (!gp) return bad(WX_ERR_INVALID, grid_name ? std::string("no grid named ") + grid_name : "file has no grid");
+    const Grid &g = *gp;
+    // Grid header (read.rs:123-164).
+    r.seek(g.grid_pos);
+    if (version >= kNodeMaskCompression) r.get<uint32_t>();
+    read_metadata(r);
+    const std::string map = r.lstr();
+    if (map == "UniformScaleMap") r.skip(5 * 24);
+    else if (map == "UniformScaleTranslateMap" || map == "ScaleTranslateMap") r.skip(6 * 24);
+    else return bad(WX_ERR_UNSUPPORTED, "unsupported transform " + map);
+    // Tree topology (read.rs:270-349).
+    if (r.get<uint32_t>() != 1) return bad(WX_ERR_UNSUPPORTED, "multi-buffer trees");
+    r.get<uint32_t>();  // background
+    const uint32_t ntiles = r.get<uint32_t>(), nnode5 = r.get<uint32_t>();
+    r.skip((long)ntiles * (12 + 4 + 1));  // root tiles are invisible to masks()/origins()
+    struct N4 {
+        std::vector<uint64_t> kid, val;
+        std::vector<std::vector<uint64_t>> leaves;
+    };
+    struct N5 {
+        wx::I3 o;
+        std::vector<uint64_t> kid, val;
+        std::vector<N4> kids;
+    };
+    std::map<wx::I3, N5> n5s;  // sorted root keys, as masks()/origins() iterate them
+    for (uint32_t i = 0; i < nnode5 && r.ok; i++) {
+        N5 n;
+        for (int a = 0; a < 3; a++) n.o[a] = wx::node_origin(r.get<int32_t>(), wx::kN5Total);
+        n.kid.resize(wx::kN5Words);
+        n.val.resize(wx::kN5Words);
+        r.bytes(n.kid.data(), wx::kN5Words * 8);
+        r.bytes(n.val.data(), wx::kN5Words * 8);
+        size_t size = wx::kN5Slots;
+        if (version < kNodeMaskCompression) {
+            size = 0;
+            for (uint64_t w : n.kid) size += 64 - (size_t)__builtin_popcountll(w);
+        }
+        if (!skip_compressed(r, version, g, size, n.val)) break;
+        for (uint32_t s5 = 0; s5 < wx::kN5Slots && r.ok; s5++) {
+            if (!wx::test_bit(n.kid.data(), s5)) continue;
+            N4 c;
+            c.kid.resize(wx::kN4Words);
+            c.val.resize(wx::kN4Words);
+            r.bytes(c.kid.data(), wx::kN4Words * 8);
+            r.bytes(c.val.data(), wx::kN4Words * 8);
+            size_t size4 = wx::kN4Slots;
+            if (version < kNodeMaskCompression) {
+                size4 = 0;
+                for (uint64_t w : c.kid) size4 += 64 - (size_t)__builtin_popcountll(w);
+            }
+            if (!skip_compressed(r, version, g, size4, c.val)) break;
+            for (uint32_t s4 = 0; s4 < wx::kN4Slots && r.ok; s4++) {
+                if (!wx::test_bit(c.kid.data(), s4)) continue;
+                std::vector<uint64_t> m(wx::kN3Words);
+                r.bytes(m.data(), wx::kN3Words * 8);
+                c.leaves.push_back(std::move(m));
+            }
+            n.kids.push_back(std::move(c));
+        }
+        if (n5s.count(n.o)) return bad(WX_ERR_INVALID, "duplicate root key");
+        n5s.emplace(n.o, std::move(n));
+    }
+    if (!r.ok) return bad(r.err.find("supported") != std::string::npos ? WX_ERR_UNSUPPORTED : WX_ERR_INVALID, r.err);
+    // masks()/origins() in DFS order (vdb345.rs:108-161).
+    std::vector<uint32_t> k5, v5, k4, v4, v3;
+    std::vector<int32_t> org;
+    auto put = [](std::vector<uint32_t> &dst, const std::vector<uint64_t> &src) {
+        for (uint64_t w : src) {
+            dst.push_back((uint32_t)w);
+            dst.push_back((uint32_t)(w >> 32));
+        }
+    };
+    for (auto &kv : n5s) {
+        put(k5, kv.second.kid);
+        put(v5, kv.second.val);
+        org.insert(org.end(), {kv.first[0], kv.first[1], kv.first[2], 0});
+        for (auto &c : kv.second.kids) {
+            put(k4, c.kid);
+            put(v4, c.val);
+            for (auto &m : c.leaves) put(v3, m);
+        }
+    }
+    const int rc = wx_topology_from_masks(k5.data(), v5.data(), n5s.size(), k4.data(), v4.data(), k4.size() / 128,
+                                          v3.data(), v3.size() / 16, org.data(), 4, out);
+    if (rc != WX_OK) return rc;
+    if (info) {
+        memset(info, 0, sizeof *info);
+        info->file_version = version;
+        info->compression = g.compression;
+        info->half_float = g.meta.half ? 1u : 0u;
+        info->file_voxel_count = g.meta.voxel_count;
+        snprintf(info->grid_name, sizeof info->grid_name, "%s", g.name.c_str());
+    }
+    return WX_OK;
+}
