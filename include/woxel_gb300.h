@@ -198,7 +198,7 @@ int wx_batch_destroy(wx_batch *batch);
  * caller must serialise them. The call blocks until earlier work on `stream`
  * is done, because the frame table is copied from pageable host memory. */
 #define WX_NOALLOC_MAX_FRAMES 256
-#define WX_NOALLOC_SCRATCH_BYTES 88320 /* 256 + 256 frames x 344-byte table entries */
+#define WX_NOALLOC_SCRATCH_BYTES 90368 /* 256 + 256 frames x 352-byte table entries */
 int wx_render_batch_noalloc(const wx_frame *frames, uint32_t n, void *stream);
 
 /* ---- serving: continuous batching of render requests (no counterpart in the

@@ -87,6 +87,25 @@ def test_dropin_view_upload_equals_native_build(cuda_ctx):
     compare(r1, h1, ro, ho, label="dropin")
 
 
+def test_large_leaf_distances_use_the_overflow_table(cuda_ctx):
+    """Leaf texels >= 255 (possible in a hand-made view) are stored exactly beside the byte pool."""
+    rng = np.random.default_rng(12)
+    topo = wx.Topology.from_voxels(rng.integers(-120, 120, size=(3000, 3)).astype(np.int32))
+    marker = 0x7FFFFFFF
+    view = topo.view(value_texel=marker)
+    a3 = view["atlas"][2].copy()
+    inactive = np.nonzero(a3 != marker)[0]
+    pick = rng.choice(inactive, size=min(4000, inactive.size), replace=False)
+    a3[pick] = rng.choice(np.array([254, 255, 256, 300, 4097, 70000, 4000000000], np.uint32), size=pick.size)
+    view["atlas"] = [view["atlas"][0], view["atlas"][1], a3]
+    grid = cuda_ctx.upload_view(view)
+    for eye, mode in [((150.0, 90.0, -200.0), 3), ((-40.0, 180.0, 160.0), 0)]:
+        st = wx.state_build(eye=eye, target=(0, 0, 0), aspect=1.0, fovy=70.0, width=96.0, mode=mode)
+        rg, hg = gpu_render(cuda_ctx, grid, st, 96, 96)
+        ro, ho = oracle_render(view, st, 96, 96)
+        compare(rg, hg, ro, ho, label=f"overflow/mode{mode}")
+
+
 def test_host_buffers_match_device_buffers(cuda_ctx, sphere64):
     _, view, grid = sphere64
     st = wx.state_build(eye=(100, 40, 120), target=(0, 0, 0), aspect=4 / 3, fovy=60.0, width=320.0, mode=3)

@@ -330,7 +330,7 @@ def render_batch_noalloc(frames: Sequence, stream=None) -> None:
     """wx_render_batch_noalloc: a batch rendered without any allocation or context.
 
     For callers that cannot allocate device memory while rendering; scratch is a
-    fixed 88,320-byte device array inside the library (at most 256 frames a call).
+    fixed 90,368-byte device array inside the library (at most 256 frames a call).
     The first call on a device sets that device up; overlapping calls race.
     """
     arr = Context._frames(frames)

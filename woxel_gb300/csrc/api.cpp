@@ -5,10 +5,15 @@
 //   o5     n5 x int4         N5 origins (root keys) in DFS order
 //   slot5  n5 x 32768 u32    per N4-sized slot: child flag|N4 index, or skip distance
 //   slot4  n4 x  4096 u32    per N3-sized slot: child flag|N3 index, or skip distance
-//   slot3  n3 x   512 u32    per voxel: skip distance, 0 for an active voxel
+//   leaf   n3 x   512 u8     per voxel: 0 for an active voxel (a hit), else the skip
+//                            distance, 255 meaning "at least 255: look it up in ovf"
+//   ovf    n_ovf x (u32,u32) (voxel key = leaf << 9 | offset, exact distance), sorted
 // A slot word folds the reference's three reads per level (child-mask word,
 // value-mask word, atlas texel; raycast.comp.wgsl:422-429, :453-461,
-// :483-489) into one 4-byte load that decides hit / descend / skip.
+// :483-489) into one load that decides hit / descend / skip. Leaf distances
+// produced by compute_sdf are small (bounded by the extent of a cluster of
+// leaves), so one byte per voxel keeps the leaf pool at a quarter of the
+// reference's texel bytes while the overflow table keeps any u32 exact.
 
 #include <cuda_runtime.h>
 
@@ -93,34 +98,6 @@ bool device_accessible(const void *p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-// Allocate one device block for the pools and fill the DevGrid pointers.
-int alloc_grid(wx_ctx *ctx, uint64_t n5, uint64_t n4, uint64_t n3, wx_grid **out) {
-    auto *gr = new (std::nothrow) wx_grid();
-    if (!gr) return fail(ctx, WX_ERR_OOM, "host allocation failed");
-    auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    const size_t b_o5 = align(std::max<uint64_t>(n5, 1) * 16), b5 = align(n5 * 32768ull * 4),
-                 b4 = align(n4 * 4096ull * 4), b3 = align(n3 * 512ull * 4);
-    gr->bytes = b_o5 + b5 + b4 + b3;
-    gr->device = ctx->device;
-    cudaError_t e = cudaMalloc(&gr->dev, gr->bytes);
-    if (e != cudaSuccess) {
-        delete gr;
-        return cuda_fail(ctx, e, "cudaMalloc(node pools)");
-    }
-    char *b = static_cast<char *>(gr->dev);
-    gr->g.o5 = reinterpret_cast<const int4 *>(b);
-    gr->g.slot5 = reinterpret_cast<const uint32_t *>(b + b_o5);
-    gr->g.slot4 = reinterpret_cast<const uint32_t *>(b + b_o5 + b5);
-    gr->g.slot3 = reinterpret_cast<const uint32_t *>(b + b_o5 + b5 + b4);
-    gr->g.n5 = (uint32_t)n5;
-    gr->info.n5 = n5;
-    gr->info.n4 = n4;
-    gr->info.n3 = n3;
-    gr->info.device_bytes = gr->bytes;
-    *out = gr;
-    return WX_OK;
-}
-
 template <class F>
 void parallel_chunks(size_t n, F f) {
     unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -139,6 +116,76 @@ void parallel_chunks(size_t n, F f) {
 
 // Tiles of tile_w x (32 / tile_w) pixels over the dispatched region
 // 8*floor(w/8) x 4*floor(h/4) (wgpu_context.rs:281).
+// Pack the per-voxel u32 leaf distances into bytes plus the overflow table,
+// allocate one device block for all pools and upload them.
+int upload_pools(wx_ctx *ctx, const std::vector<int4> &o5, const uint32_t *s5, const uint32_t *s4, const uint32_t *s3,
+                 uint64_t n5, uint64_t n4, uint64_t n3, wx_grid **out) {
+    // The kernels address each pool with a 32-bit element index (node << log2 slots | slot).
+    if (n5 > (1u << 17) || n4 > (1u << 20) || n3 > (1u << 23))
+        return fail(ctx, WX_ERR_UNSUPPORTED,
+                    "grid too large: at most 131072 N5, 1048576 N4 and 8388608 N3 nodes");
+    std::vector<uint8_t> leaf;
+    std::vector<uint2> ovf;
+    try {
+        leaf.resize(n3 * wx::kN3Slots);
+        const unsigned np = n3 < 4096 ? 1u : std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        std::vector<std::vector<uint2>> parts(np);
+        const size_t chunk = (n3 + np - 1) / np;
+        auto pack = [&](unsigned p) {
+            for (size_t k = p * chunk; k < std::min<size_t>(n3, (p + 1) * chunk); k++)
+                for (uint32_t s = 0; s < wx::kN3Slots; s++) {
+                    const uint32_t d = s3[k * wx::kN3Slots + s];
+                    leaf[k * wx::kN3Slots + s] = (uint8_t)std::min<uint32_t>(d, 255u);
+                    if (d >= 255u) parts[p].push_back(make_uint2((uint32_t)(k << 9) | s, d));
+                }
+        };
+        std::vector<std::thread> th;
+        for (unsigned p = 1; p < np; p++) th.emplace_back(pack, p);
+        pack(0);
+        for (auto &t : th) t.join();
+        for (auto &p : parts) ovf.insert(ovf.end(), p.begin(), p.end());  // ascending keys
+    } catch (...) {
+        return fail(ctx, WX_ERR_OOM, "host allocation failed while packing leaves");
+    }
+    auto *gr = new (std::nothrow) wx_grid();
+    if (!gr) return fail(ctx, WX_ERR_OOM, "host allocation failed");
+    auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t b_o5 = align(std::max<uint64_t>(n5, 1) * 16), b5 = align(n5 * 32768ull * 4),
+                 b4 = align(n4 * 4096ull * 4), b3 = align(n3 * 512ull), bo = align(ovf.size() * 8);
+    gr->bytes = b_o5 + b5 + b4 + b3 + bo;
+    gr->device = ctx->device;
+    cudaError_t e = cudaMalloc(&gr->dev, gr->bytes);
+    if (e != cudaSuccess) {
+        delete gr;
+        return cuda_fail(ctx, e, "cudaMalloc(node pools)");
+    }
+    char *b = static_cast<char *>(gr->dev);
+    gr->g.o5 = reinterpret_cast<const int4 *>(b);
+    gr->g.slot5 = reinterpret_cast<const uint32_t *>(b + b_o5);
+    gr->g.slot4 = reinterpret_cast<const uint32_t *>(b + b_o5 + b5);
+    gr->g.leaf = reinterpret_cast<const uint8_t *>(b + b_o5 + b5 + b4);
+    gr->g.ovf = reinterpret_cast<const uint2 *>(b + b_o5 + b5 + b4 + b3);
+    gr->g.n5 = (uint32_t)n5;
+    gr->g.n_ovf = (uint32_t)ovf.size();
+    gr->info.n5 = n5;
+    gr->info.n4 = n4;
+    gr->info.n3 = n3;
+    gr->info.device_bytes = gr->bytes;
+    if (e == cudaSuccess && n5) e = cudaMemcpy((void *)gr->g.o5, o5.data(), n5 * 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n5) e = cudaMemcpy((void *)gr->g.slot5, s5, n5 * 32768ull * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n4) e = cudaMemcpy((void *)gr->g.slot4, s4, n4 * 4096ull * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n3) e = cudaMemcpy((void *)gr->g.leaf, leaf.data(), leaf.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !ovf.empty())
+        e = cudaMemcpy((void *)gr->g.ovf, ovf.data(), ovf.size() * 8, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(gr->dev);
+        delete gr;
+        return cuda_fail(ctx, e, "cudaMemcpy(node pools)");
+    }
+    *out = gr;
+    return WX_OK;
+}
+
 wxk::Job make_job(const wx_grid *grid, const wx_state_uniform &s, uint32_t width, uint32_t height, uint32_t *rgba,
                   wx_hit *hits, uint32_t tile_begin, int tile_w) {
     wxk::Job j;
@@ -375,19 +422,8 @@ int wx_grid_build(wx_ctx *ctx, wx_topology *t, wx_grid **out) {
     }
     if (too_far) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_build: tile distance >= 2^31");
     wx_grid *gr = nullptr;
-    rc = alloc_grid(ctx, n5, n4, n3, &gr);
+    rc = upload_pools(ctx, o5, s5.data(), s4.data(), t->slot3.data(), n5, n4, n3, &gr);
     if (rc != WX_OK) return rc;
-    cudaError_t e = cudaSuccess;
-    if (e == cudaSuccess && n5) e = cudaMemcpy((void *)gr->g.o5, o5.data(), n5 * 16, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && n5) e = cudaMemcpy((void *)gr->g.slot5, s5.data(), s5.size() * 4, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && n4) e = cudaMemcpy((void *)gr->g.slot4, s4.data(), s4.size() * 4, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && n3)
-        e = cudaMemcpy((void *)gr->g.slot3, t->slot3.data(), n3 * 512ull * 4, cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-        cudaFree(gr->dev);
-        delete gr;
-        return cuda_fail(ctx, e, "cudaMemcpy(node pools)");
-    }
     gr->info.active_voxels = wx_topology_active_voxels(t);
     *out = gr;
     return WX_OK;
@@ -476,18 +512,8 @@ int wx_grid_upload(wx_ctx *ctx, const wx_vdb345_view *v, wx_grid **out) {
     if (bad == 1) return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: child index in atlas out of range");
     if (bad == 2) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_upload: internal tile distance >= 2^31");
     wx_grid *gr = nullptr;
-    int rc = alloc_grid(ctx, n5, n4, n3, &gr);
+    int rc = upload_pools(ctx, o5, s5.data(), s4.data(), s3.data(), n5, n4, n3, &gr);
     if (rc != WX_OK) return rc;
-    cudaError_t e = cudaSuccess;
-    if (e == cudaSuccess && n5) e = cudaMemcpy((void *)gr->g.o5, o5.data(), n5 * 16, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && n5) e = cudaMemcpy((void *)gr->g.slot5, s5.data(), s5.size() * 4, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && n4) e = cudaMemcpy((void *)gr->g.slot4, s4.data(), s4.size() * 4, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && n3) e = cudaMemcpy((void *)gr->g.slot3, s3.data(), s3.size() * 4, cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-        cudaFree(gr->dev);
-        delete gr;
-        return cuda_fail(ctx, e, "cudaMemcpy(node pools)");
-    }
     uint64_t act = 0;
     for (uint64_t w = 0; w < n3 * 16; w++) act += (uint64_t)__builtin_popcount(v->vals3[w]);
     gr->info.active_voxels = act;

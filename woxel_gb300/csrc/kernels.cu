@@ -57,8 +57,11 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
 }
 
 // One warp per tile, tiles in launch order.
-// Blocks of at most 256 threads with 64 registers a thread: 32 resident warps per SM.
-#define WX_RAY_BOUNDS __launch_bounds__(256, 4)
+// Blocks of at most 256 threads, at least 5 resident: 48 registers a thread and
+// 40 resident warps per SM. Measured on GB300 (2000-sphere frames): 48
+// registers beat 64 (32 warps) by 2% and 80 (24 warps) by 17% despite a few
+// spills outside the march loop; 40 registers spill too much.
+#define WX_RAY_BOUNDS __launch_bounds__(256, 5)
 
 __global__ void WX_RAY_BOUNDS k_pixel(const __grid_constant__ Job job, uint32_t ntiles) {
     const uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -200,7 +203,7 @@ cudaError_t check_division(uint32_t max_m, unsigned long long *out_dev, cudaStre
 // deadline). wx_render_batch needs a context whose scratch (queue counters,
 // frame table) comes from cudaMalloc. This entry point instead keeps its
 // scratch in the fixed device array below, which the library declares
-// statically: every GPU that loads the library holds these 88,320 bytes until
+// statically: every GPU that loads the library holds these 90,368 bytes until
 // the process exits. Layout: the tile-queue counter at byte 0, the frame
 // (job) table from byte 256, room for WX_NOALLOC_MAX_FRAMES frames.
 // ---------------------------------------------------------------------------

@@ -21,7 +21,8 @@ namespace wxd {
 constexpr uint32_t kChild = 0x80000000u;
 constexpr uint32_t kMaxSteps = 1000u;  // HDDA_MAX_RAY_STEPS, raycast.comp.wgsl:82
 
-// o5: N5 origins (x, y, z, 0) in DFS order; slot5/4/3: n5*32768, n4*4096, n3*512 slot words.
+// o5: N5 origins in DFS order; slot5/slot4: n5*32768 and n4*4096 slot words;
+// leaf: n3*512 voxel bytes (0 hit, 1..254 distance, 255 = exact distance in ovf).
 using DevGrid = wxk::DevGrid;
 
 // RN(1 / (2j + 1)) for j < kRcpOdd: filled once per device from host IEEE
@@ -101,9 +102,11 @@ struct Ray {
     float dx, dy, dz;
     float ix, iy, iz;
     float ax, ay, az;  // step01
+    float nx, ny, nz;  // 4e-4 * step
     int lx, ly, lz;
     uint32_t np, i5, i4, i3;
-    uint32_t mask, i;
+    uint32_t i;
+    bool mx, my, mz;   // mask of the last step
 };
 
 __device__ __forceinline__ void ray_init(Ray &r, F3 src, F3 dir) {
@@ -111,10 +114,15 @@ __device__ __forceinline__ void ray_init(Ray &r, F3 src, F3 dir) {
     r.dx = dir.x; r.dy = dir.y; r.dz = dir.z;
     r.ix = __frcp_rn(dir.x); r.iy = __frcp_rn(dir.y); r.iz = __frcp_rn(dir.z);
     r.ax = pmax(0.0f, sign11(dir.x)); r.ay = pmax(0.0f, sign11(dir.y)); r.az = pmax(0.0f, sign11(dir.z));
+    r.nx = (r.ax - 0.5f) * 8e-4f; r.ny = (r.ay - 0.5f) * 8e-4f; r.nz = (r.az - 0.5f) * 8e-4f;
     r.lx = r.ly = r.lz = 0;
     r.np = 0; r.i5 = r.i4 = r.i3 = 0;
-    r.mask = 0;
+    r.mx = r.my = r.mz = false;
     r.i = 0;
+}
+
+__device__ __forceinline__ uint32_t ray_mask(const Ray &r) {
+    return (uint32_t)r.mx | ((uint32_t)r.my << 1) | ((uint32_t)r.mz << 2);
 }
 
 // A ray needs the NaN-aware step when 1/dir can be infinite (a direction
@@ -123,6 +131,18 @@ __device__ __forceinline__ void ray_init(Ray &r, F3 src, F3 dir) {
 // number and min/argmin need no NaN handling.
 __device__ __forceinline__ bool ray_needs_nan_checks(F3 dir) {
     return !(fminf(fminf(fabsf(dir.x), fabsf(dir.y)), fabsf(dir.z)) >= 0x1p-126f);
+}
+
+// Exact distance of a leaf voxel whose byte is 255 (distance >= 255): binary
+// search of the grid's sorted overflow table, which holds every such voxel.
+__device__ __noinline__ uint32_t leaf_overflow(const DevGrid &g, uint32_t key) {
+    uint32_t lo = 0, hi = g.n_ovf;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&g.ovf[mid].x) < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo < g.n_ovf ? __ldg(&g.ovf[lo].y) : 255u;
 }
 
 // One loop iteration of hdda_ray. Returns 0xFF while the march continues,
@@ -158,7 +178,7 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     if (lvl == 5) {  // get_vdb_leaf_from_node5 (:415-444)
         const uint32_t off = ((((uint32_t)x >> 7) & 31u) << 10) | ((((uint32_t)y >> 7) & 31u) << 5) |
                              (((uint32_t)z >> 7) & 31u);
-        const uint32_t w = __ldg(g.slot5 + ((size_t)r.i5 << 15) + off);
+        const uint32_t w = __ldg(g.slot5 + ((r.i5 << 15) | off));
         r.np = 1;
         if (w & kChild) {
             r.i4 = w & ~kChild;
@@ -170,7 +190,7 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     if (lvl == 4) {  // get_vdb_leaf_from_node4 (:446-475)
         const uint32_t off = ((((uint32_t)x >> 3) & 15u) << 8) | ((((uint32_t)y >> 3) & 15u) << 4) |
                              (((uint32_t)z >> 3) & 15u);
-        const uint32_t w = __ldg(g.slot4 + ((size_t)r.i4 << 12) + off);
+        const uint32_t w = __ldg(g.slot4 + ((r.i4 << 12) | off));
         r.np = 2;
         if (w & kChild) {
             r.i3 = w & ~kChild;
@@ -180,8 +200,9 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
         }
     }
     if (lvl == 3) {  // get_vdb_leaf_from_node3 (:477-494)
-        const uint32_t off = (((uint32_t)x & 7u) << 6) | (((uint32_t)y & 7u) << 3) | ((uint32_t)z & 7u);
-        dist = __ldg(g.slot3 + ((size_t)r.i3 << 9) + off);
+        const uint32_t key = (r.i3 << 9) | (((uint32_t)x & 7u) << 6) | (((uint32_t)y & 7u) << 3) | ((uint32_t)z & 7u);
+        dist = __ldg(g.leaf + key);
+        if (dist == 255u) dist = leaf_overflow(g, key);
         r.np = 3;
     }
     if (dist == 0u) return 0u;
@@ -228,11 +249,13 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     r.px = r.px + t * r.dx;
     r.py = r.py + t * r.dy;
     r.pz = r.pz + t * r.dz;
-    r.mask = (uint32_t)mx | ((uint32_t)my << 1) | ((uint32_t)mz << 2);
+    r.mx = mx;
+    r.my = my;
+    r.mz = mz;
     // p += (4e-4 * step) * f32(mask)  (:122)
-    r.px = r.px + ((r.ax - 0.5f) * 8e-4f) * (mx ? 1.0f : 0.0f);
-    r.py = r.py + ((r.ay - 0.5f) * 8e-4f) * (my ? 1.0f : 0.0f);
-    r.pz = r.pz + ((r.az - 0.5f) * 8e-4f) * (mz ? 1.0f : 0.0f);
+    r.px = r.px + r.nx * (mx ? 1.0f : 0.0f);
+    r.py = r.py + r.ny * (my ? 1.0f : 0.0f);
+    r.pz = r.pz + r.nz * (mz ? 1.0f : 0.0f);
     r.i++;
     return 0xFFu;
 }
@@ -268,7 +291,7 @@ __device__ __forceinline__ March hdda(const DevGrid &g, F3 src, F3 dir) {
     m.np = r.np;
     m.node = ray_node(r);
     m.i = r.i;
-    m.mask = r.mask;
+    m.mask = ray_mask(r);
     return m;
 }
 

@@ -9,12 +9,14 @@
 
 namespace wxk {
 
-struct DevGrid {  // same layout as wxd::DevGrid
-    const int4 *o5;
-    const uint32_t *slot5;
-    const uint32_t *slot4;
-    const uint32_t *slot3;
-    uint32_t n5;
+// Device node pools of one grid (see api.cpp for the layout).
+struct DevGrid {
+    const int4 *o5;          // N5 origins
+    const uint32_t *slot5;   // N5 slot words
+    const uint32_t *slot4;   // N4 slot words
+    const uint8_t *leaf;     // N3: one byte per voxel, 0 hit, 1..254 distance, 255 = see ovf
+    const uint2 *ovf;        // (voxel key = leaf << 9 | offset, distance), sorted by key
+    uint32_t n5, n_ovf;
 };
 
 // One frame of one grid: the unit the persistent kernels draw ray tiles from.
