@@ -44,6 +44,18 @@ def test_sphere_config1():
     compare_views(topo)
 
 
+def test_parallel_wavefront_equals_sequential_sweep():
+    """The multi-threaded dependency-ordered sweep gives the single-threaded Gauss-Seidel result."""
+    views = []
+    for nthreads in (1, 8):
+        topo = wx.Topology.spheres(count=150, rmin=4.0, rmax=30.0, lo=-300.0, hi=300.0, band=3.0, seed=7)
+        assert topo.counts[2] > 5000  # takes the parallel path
+        topo.sdf(nthreads)
+        views.append(topo.atlas())
+    for i in range(3):
+        np.testing.assert_array_equal(views[0][0][i], views[1][0][i], err_msg=f"atlas {i}")
+
+
 def test_active_tiles_count_as_empty():
     """Value-mask bits on N4/N5 slots (active tiles) are tiles for the SDF but hits for the march."""
     topo = wx.Topology.from_voxels(np.array([[3, 3, 3], [300, 40, 40]], np.int32))

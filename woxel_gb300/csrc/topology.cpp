@@ -20,6 +20,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
+#include <memory>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -76,8 +78,17 @@ class OriginIndex {
 // One level of compute_sdf. Containers (nodes of this level) are given in DFS
 // order with their origins in voxels and extent 2^span_log2; cells hold 0 for
 // solid slots and kSdfInf for tiles on entry, final distances on exit.
+//
+// The reference sweeps the containers one after the other (forward in DFS
+// order, then backward). A container's sweep reads only itself and its 26
+// neighbours, so the sequential order only matters between neighbours: in
+// the forward pass a container must see its lower-index neighbours finished
+// and its higher-index neighbours untouched (mirrored backward). With nthreads
+// > 1 the sweeps run as a wavefront over that dependency DAG: a container
+// becomes ready when all its earlier neighbours are done, so every container
+// reads exactly the values the sequential order gives it.
 template <int L>
-static void chamfer_level(const std::vector<I3> &org, int span_log2, uint32_t *dist) {
+static void chamfer_level(const std::vector<I3> &org, int span_log2, uint32_t *dist, int nthreads) {
     constexpr int D = 1 << L, P = D + 2, N = D * D * D;
     const size_t nc = org.size();
     if (nc == 0) return;
@@ -91,10 +102,9 @@ static void chamfer_level(const std::vector<I3> &org, int span_log2, uint32_t *d
                                        : index.find(org[c][0] + dx * span, org[c][1] + dy * span,
                                                     org[c][2] + dz * span);
         }
-    std::vector<uint32_t> buf((size_t)P * P * P);
     auto bidx = [](int x, int y, int z) { return ((x + 1) * P + (y + 1)) * P + (z + 1); };
 
-    auto fill = [&](size_t c) {
+    auto fill = [&](size_t c, uint32_t *buf) {
         for (int k = 0; k < 27; k++) {
             const int d[3] = {k / 9 - 1, (k / 3) % 3 - 1, k % 3 - 1};
             int lo[3], hi[3], src[3];
@@ -118,7 +128,7 @@ static void chamfer_level(const std::vector<I3> &org, int span_log2, uint32_t *d
                     }
         }
     };
-    auto store = [&](size_t c) {
+    auto store = [&](size_t c, const uint32_t *buf) {
         uint32_t *dc = dist + c * N;
         for (int x = 0; x < D; x++)
             for (int y = 0; y < D; y++)
@@ -140,7 +150,8 @@ static void chamfer_level(const std::vector<I3> &org, int span_log2, uint32_t *d
     fo[k] = -1;
     bo[k] = 1;
 
-    auto sweep = [&](const int *off, bool backward) {
+    auto sweep = [&](uint32_t *buf, bool backward) {
+        const int *off = backward ? bo : fo;
         for (int s = 0; s < N; s++) {
             const int cell = backward ? N - 1 - s : s;
             const int x = cell >> (2 * L), y = (cell >> L) & (D - 1), z = cell & (D - 1);
@@ -151,15 +162,65 @@ static void chamfer_level(const std::vector<I3> &org, int span_log2, uint32_t *d
             if (m + 1u < *self) *self = m + 1u;
         }
     };
-    for (size_t c = 0; c < nc; c++) {
-        fill(c);
-        sweep(fo, false);
-        store(c);
+    auto process = [&](size_t c, uint32_t *buf, bool backward) {
+        fill(c, buf);
+        sweep(buf, backward);
+        store(c, buf);
+    };
+
+    if (nthreads <= 1 || nc < 256) {
+        std::vector<uint32_t> buf((size_t)P * P * P);
+        for (size_t c = 0; c < nc; c++) process(c, buf.data(), false);
+        for (size_t c = nc; c-- > 0;) process(c, buf.data(), true);
+        return;
     }
-    for (size_t c = nc; c-- > 0;) {
-        fill(c);
-        sweep(bo, true);
-        store(c);
+    std::unique_ptr<std::atomic<uint32_t>[]> indeg(new std::atomic<uint32_t>[nc]);
+    for (int pass = 0; pass < 2; pass++) {
+        const bool backward = pass == 1;
+        // A neighbour comes before c in this pass's order when its index is smaller
+        // (forward) or larger (backward).
+        auto before = [&](uint32_t n, size_t c) { return backward ? n > c : n < c; };
+        std::vector<uint32_t> ready;
+        for (size_t c = 0; c < nc; c++) {
+            uint32_t deg = 0;
+            for (int j = 0; j < 27; j++) {
+                const uint32_t n = nb[c * 27 + j];
+                if (j != 13 && n != UINT32_MAX && before(n, c)) deg++;
+            }
+            indeg[c].store(deg, std::memory_order_relaxed);
+            if (deg == 0) ready.push_back((uint32_t)c);
+        }
+        std::mutex mu;
+        std::condition_variable cv;
+        size_t done = 0;
+        auto worker = [&] {
+            std::vector<uint32_t> buf((size_t)P * P * P);
+            std::unique_lock<std::mutex> lk(mu);
+            for (;;) {
+                cv.wait(lk, [&] { return !ready.empty() || done == nc; });
+                if (ready.empty()) return;
+                const uint32_t c = ready.back();
+                ready.pop_back();
+                lk.unlock();
+                process(c, buf.data(), backward);
+                uint32_t woke[26];
+                int nw = 0;
+                for (int j = 0; j < 27; j++) {
+                    const uint32_t n = nb[(size_t)c * 27 + j];
+                    if (j == 13 || n == UINT32_MAX || before(n, c)) continue;
+                    if (indeg[n].fetch_sub(1, std::memory_order_acq_rel) == 1) woke[nw++] = n;
+                }
+                lk.lock();
+                for (int w = 0; w < nw; w++) ready.push_back(woke[w]);
+                done++;
+                if (nw > 1 || done == nc) cv.notify_all();
+                else if (nw == 1) cv.notify_one();
+            }
+        };
+        std::vector<std::thread> th;
+        for (int t = 1; t < nthreads; t++) th.emplace_back(worker);
+        worker();
+        for (auto &t : th) t.join();
     }
 }
 
@@ -387,7 +448,6 @@ int wx_topology_masks(const wx_topology *t, uint32_t *kids5, uint32_t *vals5, ui
 int wx_topology_sdf(wx_topology *t, int nthreads) {
     if (!t) return WX_ERR_INVALID;
     if (t->has_sdf) return WX_OK;
-    (void)nthreads;
     try {
         t->d5.resize(t->n5() * kN5Slots);
         t->d4.resize(t->n4() * kN4Slots);
@@ -401,19 +461,18 @@ int wx_topology_sdf(wx_topology *t, int nthreads) {
             for (uint32_t s = 0; s < slots; s++)
                 d[c * slots + s] = test_bit(&solid[c * (slots / 64)], s) ? 0u : kSdfInf;
     };
-    // The three levels are independent sweeps; run them concurrently.
-    std::thread th5([&] {
+    // The three levels are independent sweeps; the small N5/N4 levels run on
+    // one helper thread while the leaf level uses the remaining workers.
+    if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+    std::thread upper([&] {
         init(t->kid5, kN5Slots, t->d5);
-        chamfer_level<5>(t->o5, kN5Total, t->d5.data());
-    });
-    std::thread th4([&] {
+        chamfer_level<5>(t->o5, kN5Total, t->d5.data(), 1);
         init(t->kid4, kN4Slots, t->d4);
-        chamfer_level<4>(t->o4, kN4Total, t->d4.data());
+        chamfer_level<4>(t->o4, kN4Total, t->d4.data(), std::max(1, nthreads / 4));
     });
     init(t->val3, kN3Slots, t->slot3);
-    chamfer_level<3>(t->o3, kN3Total, t->slot3.data());
-    th4.join();
-    th5.join();
+    chamfer_level<3>(t->o3, kN3Total, t->slot3.data(), std::max(1, nthreads - 1));
+    upper.join();
     t->has_sdf = true;
     return WX_OK;
 }
