@@ -271,7 +271,7 @@ int wx_server_replay(wx_server *srv, const wx_request *reqs, const double *arriv
 int wx_server_destroy(wx_server *srv);
 
 /* Exhaustive GPU check of the kernels' fast floor(p / size) path against IEEE
- * division: every odd divisor m < max_m (<= 4096) and every significand of
+ * division: every divisor m < max_m (<= 4096) and every significand of
  * [1,2) and [-2,-1). out = {mismatches, first bad m, its x bits}. */
 int wx_check_division(wx_ctx *ctx, uint32_t max_m, uint64_t out[3]);
 

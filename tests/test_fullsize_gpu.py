@@ -1,0 +1,79 @@
+"""Parity at the benchmark's full sizes, on sampled tiles and size-independent properties.
+
+* 2000-sphere grid (476k leaves), 1920x1080 frames: random 8x4 tiles against the
+  oracle; batched launch == per-frame launches; repeated renders identical.
+* 4096^3 noise grid (2.68M leaves, 2% occupancy, p=0.5 voxels), 3840x2160, mode 0
+  (first active voxel): random tiles against the oracle.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as orc
+import woxel_gb300 as wx
+from parity import compare, gpu_render
+from woxel_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def tile_mask(w, h, tiles):
+    m = np.zeros((h, w), bool)
+    tx = w // 8
+    for t in tiles:
+        x0, y0 = (int(t) % tx) * 8, (int(t) // tx) * 4
+        m[y0:y0 + 4, x0:x0 + 8] = True
+    return m
+
+
+def sampled_parity(ctx, grid, view, frame, ntiles, seed):
+    st = frame.state()
+    rg, hg = gpu_render(ctx, grid, st, frame.width, frame.height)
+    rng = np.random.default_rng(seed)
+    tiles = np.sort(rng.choice((frame.width // 8) * (frame.height // 4), size=ntiles, replace=False)).astype(np.uint64)
+    ro, ho, _ = orc.render(view, wx.state_bytes(st), frame.width, frame.height, nthreads=16, hits=True, tiles=tiles)
+    m = tile_mask(frame.width, frame.height, tiles)
+    compare(rg, hg, ro, ho, where=m, label=f"{frame.grid} {frame.width}x{frame.height}")
+    return rg, hg
+
+
+@pytest.fixture(scope="module")
+def spheres(cuda_ctx):
+    topo = W.spheres_topology()
+    grid = cuda_ctx.build_grid(topo)
+    return topo, topo.view(), grid
+
+
+def test_spheres_1080p_sampled_tiles(cuda_ctx, spheres):
+    topo, view, grid = spheres
+    frames = W.spheres_frames()
+    for k in (0, 7):
+        rg, hg = sampled_parity(cuda_ctx, grid, view, frames[k], ntiles=1500, seed=k)
+        assert (wx.hit_fields(hg)["state"] == 0).mean() > 0.05
+
+
+def test_spheres_batched_equals_plain_and_repeatable(cuda_ctx, spheres):
+    _, _, grid = spheres
+    frames = W.spheres_frames()[:4]
+    outs = [torch.zeros(f.width * f.height * 4, dtype=torch.uint8, device="cuda") for f in frames]
+    cuda_ctx.render_batch([(grid, f.state(), f.width, f.height, o, None) for f, o in zip(frames, outs)])
+    torch.cuda.synchronize()
+    for f, o in zip(frames, outs):
+        a, _ = gpu_render(cuda_ctx, grid, f.state(), f.width, f.height, hits=False)
+        b, _ = gpu_render(cuda_ctx, grid, f.state(), f.width, f.height, hits=False)
+        np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(o.cpu().numpy().reshape(f.height, f.width, 4), a)
+
+
+def test_noise_4k_sampled_tiles(cuda_ctx):
+    topo = W.noise_topology()
+    n5, n4, n3 = topo.counts
+    assert abs(n3 / (512 ** 3) - 0.02) < 0.001  # 2.0% of the 8^3 leaf lattice
+    grid = cuda_ctx.build_grid(topo)
+    assert grid.info["n3"] == n3
+    view = topo.view()
+    frame = W.noise_frames()[0]
+    rg, hg = sampled_parity(cuda_ctx, grid, view, frame, ntiles=600, seed=3)
+    f = wx.hit_fields(hg)
+    hit = f["state"] == 0
+    assert hit.mean() > 0.05 and (f["level"][hit] == 3).all()  # first active voxel, always inside a leaf

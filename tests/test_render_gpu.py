@@ -19,7 +19,7 @@ def kernel(request, cuda_ctx):
 
 
 def test_fast_division_matches_ieee(cuda_ctx, kernel):
-    """Every odd divisor m < 4096 and every significand of [1,2) and [-2,-1): bit-equal to IEEE x/m."""
+    """Every divisor m < 4096 and every significand of [1,2) and [-2,-1): bit-equal to IEEE x/m."""
     if kernel != "persistent":
         pytest.skip("kernel independent")
     bad, m, xbits = cuda_ctx.check_division(4096)
@@ -104,6 +104,27 @@ def test_large_leaf_distances_use_the_overflow_table(cuda_ctx):
         rg, hg = gpu_render(cuda_ctx, grid, st, 96, 96)
         ro, ho = oracle_render(view, st, 96, 96)
         compare(rg, hg, ro, ho, label=f"overflow/mode{mode}")
+
+
+def test_root_table_and_root_scan(cuda_ctx):
+    """N5 lookup through the dense root-key table (keys with holes) and through the scan that
+    replaces it when the box of root keys exceeds 2^20 entries: both match the oracle."""
+    cube = np.stack(np.mgrid[0:40, 0:40, 0:40], -1).reshape(-1, 3)
+    near = np.concatenate([cube + 1500, cube - 1540])            # N5 keys (0,0,0) and (-1,-1,-1) only
+    far = np.array([[4096 * 1500, 4096 * 1500, 0]])              # key box 1501 x 1501 x 1
+    views = [((3500.0, 3400.0, 3600.0), (1500, 1500, 1500), 3),
+             ((-3900.0, -200.0, -3900.0), (-1500, -1500, -1500), 0),
+             ((10.0, -20.0, 30.0), (1500, 1500, 1500), 3)]     # eye in key (0,-1,0): no N5 there
+    for ijk in (near, np.concatenate([near, far])):
+        topo = wx.Topology.from_voxels(ijk.astype(np.int32))
+        view = topo.view()
+        grid = cuda_ctx.build_grid(topo)
+        for eye, target, mode in views:
+            st = wx.state_build(eye=eye, target=target, aspect=1.0, fovy=3.0, width=96.0, mode=mode)
+            rg, hg = gpu_render(cuda_ctx, grid, st, 96, 96)
+            ro, ho = oracle_render(view, st, 96, 96)
+            compare(rg, hg, ro, ho, label=f"root n5={topo.counts[0]} eye={eye}")
+            assert (wx.hit_fields(hg)["state"] == 0).mean() > 0.01
 
 
 def test_host_buffers_match_device_buffers(cuda_ctx, sphere64):

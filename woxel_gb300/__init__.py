@@ -36,11 +36,18 @@ def _ptr(a) -> Optional[int]:
 
 
 def hit_fields(hits: np.ndarray) -> dict:
-    """Decode wx_hit records: state, level, mask, steps, node, ijk = floor(p), t, shadow."""
+    """Decode wx_hit records: state, level, mask, steps, node, ijk = floor(p), t, shadow.
+
+    ijk of a position outside the int32 range (a ray that left the grid after a long
+    jump) or of a non-finite one is -2^31.
+    """
     info = hits["info"]
+    fp = np.floor(hits["p"].astype(np.float64))
+    ok = np.isfinite(fp) & (fp >= -2.0 ** 31) & (fp < 2.0 ** 31)
+    ijk = np.where(ok, fp, -2.0 ** 31).astype(np.int32)
     return {
         "state": info & 3, "level": (info >> 2) & 3, "mask": (info >> 4) & 7, "steps": (info >> 8) & 0x7FF,
-        "node": hits["node"], "ijk": np.floor(hits["p"]).astype(np.int32), "t": hits["t"],
+        "node": hits["node"], "ijk": ijk, "t": hits["t"],
         "p": hits["p"], "shadow": hits["shadow"],
     }
 

@@ -2,7 +2,10 @@
 // per-frame render, batched render (one-shot and CUDA-graph plans), tuning.
 //
 // Device layout of a grid (uploaded once, immutable afterwards):
-//   o5     n5 x int4         N5 origins (root keys) in DFS order
+//   root   2 x int4          header: {lo.x, lo.y, lo.z, dim.x}, {dim.y, dim.z, 0, use table}
+//          n5 x int4         N5 origins (root keys) in DFS order
+//          dim.x*dim.y*dim.z u32  dense root-key table over the box of N5 keys
+//                            (origin >> 12) starting at lo: N5 index + 1, 0 = none
 //   slot5  n5 x 32768 u32    per N4-sized slot: child flag|N4 index, or skip distance
 //   slot4  n4 x  4096 u32    per N3-sized slot: child flag|N3 index, or skip distance
 //   leaf   n3 x   512 u8     per voxel: 0 for an active voxel (a hit), else the skip
@@ -114,8 +117,48 @@ void parallel_chunks(size_t n, F f) {
     for (auto &x : th) x.join();
 }
 
-// Tiles of tile_w x (32 / tile_w) pixels over the dispatched region
-// 8*floor(w/8) x 4*floor(h/4) (wgpu_context.rs:281).
+// The root block: header, origins and the dense table of root keys, which
+// replaces the linear scan of get_vdb_leaf_from_nothing
+// (raycast.comp.wgsl:398-413) with one load. The scan compares
+// floor(p) & ~4095 with each origin, so only origins that are multiples of
+// 4096 can match; the table holds those, the first of equal origins winning as
+// in the scan. Boxes of more than 2^20 keys keep the scan (use table = 0).
+std::vector<int4> root_block(const std::vector<int4> &o5, uint64_t n5) {
+    constexpr uint64_t kMaxKeys = 1u << 20;
+    int lo[3] = {0, 0, 0}, hi[3] = {-1, -1, -1};
+    bool any = false;
+    for (uint64_t i = 0; i < n5; i++) {
+        const int v[3] = {o5[i].x, o5[i].y, o5[i].z};
+        if ((v[0] & 4095) || (v[1] & 4095) || (v[2] & 4095)) continue;
+        for (int a = 0; a < 3; a++) {
+            const int k = v[a] >> 12;
+            lo[a] = any ? std::min(lo[a], k) : k;
+            hi[a] = any ? std::max(hi[a], k) : k;
+        }
+        any = true;
+    }
+    uint64_t dim[3], keys = 1;
+    for (int a = 0; a < 3; a++) {
+        dim[a] = any ? (uint64_t)((int64_t)hi[a] - lo[a] + 1) : 0;
+        keys *= dim[a];
+    }
+    const bool use = keys <= kMaxKeys;
+    const uint64_t tab = use ? keys : 0;
+    std::vector<int4> b(2 + n5 + (tab + 3) / 4, make_int4(0, 0, 0, 0));
+    b[0] = make_int4(lo[0], lo[1], lo[2], (int)(use ? dim[0] : 0));
+    b[1] = make_int4((int)(use ? dim[1] : 0), (int)(use ? dim[2] : 0), 0, use ? 1 : 0);
+    for (uint64_t i = 0; i < n5; i++) b[2 + i] = o5[i];
+    auto *t = reinterpret_cast<uint32_t *>(b.data() + 2 + n5);
+    for (uint64_t i = 0; use && i < n5; i++) {
+        const int v[3] = {o5[i].x, o5[i].y, o5[i].z};
+        if ((v[0] & 4095) || (v[1] & 4095) || (v[2] & 4095)) continue;
+        const uint64_t e = ((uint64_t)((v[2] >> 12) - lo[2]) * dim[1] + (uint64_t)((v[1] >> 12) - lo[1])) * dim[0] +
+                           (uint64_t)((v[0] >> 12) - lo[0]);
+        if (!t[e]) t[e] = (uint32_t)i + 1u;
+    }
+    return b;
+}
+
 // Pack the per-voxel u32 leaf distances into bytes plus the overflow table,
 // allocate one device block for all pools and upload them.
 int upload_pools(wx_ctx *ctx, const std::vector<int4> &o5, const uint32_t *s5, const uint32_t *s4, const uint32_t *s3,
@@ -149,8 +192,15 @@ int upload_pools(wx_ctx *ctx, const std::vector<int4> &o5, const uint32_t *s5, c
     }
     auto *gr = new (std::nothrow) wx_grid();
     if (!gr) return fail(ctx, WX_ERR_OOM, "host allocation failed");
+    std::vector<int4> root;
+    try {
+        root = root_block(o5, n5);
+    } catch (...) {
+        delete gr;
+        return fail(ctx, WX_ERR_OOM, "host allocation failed");
+    }
     auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    const size_t b_o5 = align(std::max<uint64_t>(n5, 1) * 16), b5 = align(n5 * 32768ull * 4),
+    const size_t b_o5 = align(root.size() * 16), b5 = align(n5 * 32768ull * 4),
                  b4 = align(n4 * 4096ull * 4), b3 = align(n3 * 512ull), bo = align(ovf.size() * 8);
     gr->bytes = b_o5 + b5 + b4 + b3 + bo;
     gr->device = ctx->device;
@@ -160,7 +210,7 @@ int upload_pools(wx_ctx *ctx, const std::vector<int4> &o5, const uint32_t *s5, c
         return cuda_fail(ctx, e, "cudaMalloc(node pools)");
     }
     char *b = static_cast<char *>(gr->dev);
-    gr->g.o5 = reinterpret_cast<const int4 *>(b);
+    gr->g.root = reinterpret_cast<const int4 *>(b);
     gr->g.slot5 = reinterpret_cast<const uint32_t *>(b + b_o5);
     gr->g.slot4 = reinterpret_cast<const uint32_t *>(b + b_o5 + b5);
     gr->g.leaf = reinterpret_cast<const uint8_t *>(b + b_o5 + b5 + b4);
@@ -171,7 +221,7 @@ int upload_pools(wx_ctx *ctx, const std::vector<int4> &o5, const uint32_t *s5, c
     gr->info.n4 = n4;
     gr->info.n3 = n3;
     gr->info.device_bytes = gr->bytes;
-    if (e == cudaSuccess && n5) e = cudaMemcpy((void *)gr->g.o5, o5.data(), n5 * 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy((void *)gr->g.root, root.data(), root.size() * 16, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && n5) e = cudaMemcpy((void *)gr->g.slot5, s5, n5 * 32768ull * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && n4) e = cudaMemcpy((void *)gr->g.slot4, s4, n4 * 4096ull * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && n3) e = cudaMemcpy((void *)gr->g.leaf, leaf.data(), leaf.size(), cudaMemcpyHostToDevice);
@@ -186,6 +236,8 @@ int upload_pools(wx_ctx *ctx, const std::vector<int4> &o5, const uint32_t *s5, c
     return WX_OK;
 }
 
+// Tiles of tile_w x (32 / tile_w) pixels over the dispatched region
+// 8*floor(w/8) x 4*floor(h/4) (wgpu_context.rs:281).
 wxk::Job make_job(const wx_grid *grid, const wx_state_uniform &s, uint32_t width, uint32_t height, uint32_t *rgba,
                   wx_hit *hits, uint32_t tile_begin, int tile_w) {
     wxk::Job j;

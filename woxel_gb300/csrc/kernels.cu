@@ -30,11 +30,17 @@ using wxk::Job;
 __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t lane) {
     const uint32_t gx = (tl % J.tiles_x) * J.tile_w + lane % J.tile_w;
     const uint32_t gy = (tl / J.tiles_x) * J.tile_h + lane / J.tile_w;
-    if (gx >= (J.width & ~7u) || gy >= (J.height & ~3u)) return;
+    // The warp's lanes leave each march at different iterations. Without the
+    // explicit reconvergence points below they go on in small groups, each
+    // running the shading once and starting its own shadow march.
+    const bool valid = gx < (J.width & ~7u) && gy < (J.height & ~3u);
+    const uint32_t act = __ballot_sync(~0u, valid);
+    if (!valid) return;
     const wx_state_uniform &s = J.s;
     const F3 dir = primary_dir(s, gx, gy);
     const F3 eye = f3(s.eye[0], s.eye[1], s.eye[2]);
     const March hit = hdda(J.g, eye, dir);
+    __syncwarp(act);
     F3 c;
     uint32_t shadow = 0;
     if (s.render_mode[0] == 4u) {
@@ -43,12 +49,14 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
         bool need;
         F3 shadowed, src;
         c = primary_colour(s, hit, dir, &need, &shadowed, &src);
+        __syncwarp(act);  // shadow rays of the warp start together
         if (need) {
             const March sh = hdda(J.g, src, -f3(s.sun_dir[0], s.sun_dir[1], s.sun_dir[2]));
             shadow = 1u | (sh.state << 1) | (sh.i << 8);
             if (sh.state == 0u) c = shadowed;
         }
     }
+    __syncwarp(act);
     const uint32_t pix = gy * J.width + gx;
     J.rgba[pix] = pack_rgba(c);
     if (J.hits)
@@ -109,9 +117,9 @@ __global__ void k_check_div(uint32_t max_m, unsigned long long *out) {
     if (idx >= (2u << 23)) return;
     const uint32_t sig = idx & ((1u << 23) - 1u);
     const float x = __uint_as_float((idx >> 23 ? 0x80000000u : 0u) | (127u << 23) | sig);
-    for (uint32_t m = 1; m < max_m; m += 2) {
+    for (uint32_t m = 1; m < max_m; m++) {
         const float mf = __uint2float_rn(m);
-        const float a = div_fast(x, mf, g_rcp_odd[m >> 1]);
+        const float a = div_fast(x, mf, g_rcp[m]);
         const float b = __fdiv_rn(x, mf);
         if (__float_as_uint(a) != __float_as_uint(b)) {
             if (atomicAdd(&out[0], 1ull) == 0ull) {
@@ -138,12 +146,13 @@ namespace wxk {
 
 cudaError_t init_device_tables() {
     static_assert(sizeof(Job) % 8 == 0, "Job layout");
-    float h[wxd::kRcpOdd];
-    for (uint32_t j = 0; j < wxd::kRcpOdd; j++) {
-        volatile float m = (float)(2 * j + 1);
-        h[j] = 1.0f / m;  // host IEEE division, round to nearest
+    float h[wxd::kRcp];
+    h[0] = 0.0f;
+    for (uint32_t d = 1; d < wxd::kRcp; d++) {
+        volatile float m = (float)d;
+        h[d] = 1.0f / m;  // host IEEE division, round to nearest
     }
-    return cudaMemcpyToSymbol(wxd::g_rcp_odd, h, sizeof h);
+    return cudaMemcpyToSymbol(wxd::g_rcp, h, sizeof h);
 }
 
 int max_blocks_per_sm(int kernel, bool batched, int warps_per_block) {
@@ -187,7 +196,7 @@ cudaError_t launch_batched(const Job *jobs_dev, uint32_t njobs, uint32_t total_t
 cudaError_t check_division(uint32_t max_m, unsigned long long *out_dev, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(out_dev, 0, 3 * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
-    if (max_m > 2 * wxd::kRcpOdd) max_m = 2 * wxd::kRcpOdd;
+    if (max_m > wxd::kRcp) max_m = wxd::kRcp;
     k_check_div<<<(2u << 23) / 256, 256, 0, st>>>(max_m, out_dev);
     return cudaGetLastError();
 }

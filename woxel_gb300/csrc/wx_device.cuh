@@ -25,35 +25,33 @@ constexpr uint32_t kMaxSteps = 1000u;  // HDDA_MAX_RAY_STEPS, raycast.comp.wgsl:
 // leaf: n3*512 voxel bytes (0 hit, 1..254 distance, 255 = exact distance in ovf).
 using DevGrid = wxk::DevGrid;
 
-// RN(1 / (2j + 1)) for j < kRcpOdd: filled once per device from host IEEE
-// division (wxk::init_device_tables). Defined here: kernels.cu is the only
-// translation unit that includes this header.
-constexpr uint32_t kRcpOdd = 2048;
-__device__ float g_rcp_odd[kRcpOdd];
+// RN(1 / d) for 1 <= d < kRcp (entry 0 unused): filled once per device from
+// host IEEE division (wxk::init_device_tables). Defined here: kernels.cu is
+// the only translation unit that includes this header.
+constexpr uint32_t kRcp = 4096;
+__device__ float g_rcp[kRcp];
 
 __device__ __forceinline__ float pmin(float a, float b) { return (b < a || a != a) ? b : a; }
 __device__ __forceinline__ float pmax(float a, float b) { return (b > a || a != a) ? b : a; }
 __device__ __forceinline__ float sign11(float x) { return x < 0.0f ? -1.0f : 1.0f; }
 
-// RN(p / size) for the three coordinates of one step. size = dist * 2^sk =
-// m * 2^k with m odd, so y = RN(1/m) * 2^-k equals RN(1/size) exactly (a
-// power-of-two scaling). With q0 = RN(p*y), the residual e = p - q0*size is
-// exact in one FMA and RN(q0 + e*y) is the correctly rounded quotient
-// (Markstein, IBM J. Res. Dev. 34(1), 1990). The identity is invariant under
-// power-of-two scaling while every intermediate stays a normal number, so the
-// exhaustive GPU check over every odd m < 4096 and every significand of
-// [1,2) and [-2,-1) (wx_check_division) covers every exponent. The result is
-// bit-identical to __fdiv_rn except that a zero quotient may come out +0 for
-// p = -0; the march cannot observe that sign (mod = p - size*floor(q) enters
-// only size*step01 - mod, where +0 and -0 give the same value). Other cases
-// (m >= 4096, or a coordinate with |p| < 2^-64, where q0 could underflow)
+// RN(p / size) for the three coordinates of one step. size = dist * 2^sk, so
+// y = RN(1/dist) * 2^-sk equals RN(1/size) exactly (a power-of-two scaling).
+// With q0 = RN(p*y), the residual e = p - q0*size is exact in one FMA and
+// RN(q0 + e*y) is the correctly rounded quotient (Markstein, IBM J. Res. Dev.
+// 34(1), 1990). The identity is invariant under power-of-two scaling while
+// every intermediate stays a normal number, so the exhaustive GPU check over
+// every divisor d < 4096 and every significand of [1,2) and [-2,-1)
+// (wx_check_division) covers every exponent. The result is bit-identical to
+// __fdiv_rn except that a zero quotient may come out +0 for p = -0; the march
+// cannot observe that sign (mod = p - size*floor(q) enters only
+// size*step01 - mod, where +0 and -0 give the same value). Other cases
+// (dist >= 4096, or a coordinate with |p| < 2^-64, where q0 could underflow)
 // take __fdiv_rn.
 __device__ __forceinline__ float rcp_size(uint32_t dist, int sk, bool *fast) {
-    const int tz = __ffs((int)dist) - 1;  // dist >= 1, so k = tz + sk <= 43
-    const uint32_t m = dist >> tz;
-    *fast = m < 2u * kRcpOdd;
-    const float r = __ldg(&g_rcp_odd[(*fast ? m : 1u) >> 1]);
-    return r * __int_as_float((127 - tz - sk) << 23);
+    *fast = dist < kRcp;
+    const float r = __ldg(&g_rcp[*fast ? dist : 1u]);
+    return r * __int_as_float((127 - sk) << 23);  // sk <= 12
 }
 __device__ __forceinline__ float div_fast(float p, float size, float y) {
     const float q0 = p * y;
@@ -125,12 +123,18 @@ __device__ __forceinline__ uint32_t ray_mask(const Ray &r) {
     return (uint32_t)r.mx | ((uint32_t)r.my << 1) | ((uint32_t)r.mz << 2);
 }
 
-// A ray needs the NaN-aware step when 1/dir can be infinite (a direction
-// component of magnitude below 2^-126, zero, or NaN): only then can
-// idir * (size*step01 - mod) be inf * 0 = NaN. Otherwise every tMax is a
-// number and min/argmin need no NaN handling.
-__device__ __forceinline__ bool ray_needs_nan_checks(F3 dir) {
-    return !(fminf(fminf(fabsf(dir.x), fabsf(dir.y)), fabsf(dir.z)) >= 0x1p-126f);
+// A ray takes the careful step (ray_step<true>) when
+// * 1/dir can be infinite (a direction component of magnitude below 2^-126,
+//   zero, or NaN): only then can idir * (size*step01 - mod) be inf * 0 = NaN;
+//   otherwise every tMax is a number and min/argmin need no NaN handling;
+// * a source coordinate is -0: only then can a position coordinate be -0
+//   (an RN sum is -0 only when both addends are -0), and only for -0 does
+//   p + (4e-4 * step) * 0 differ from p (it gives +0 when step > 0), so
+//   elsewhere the nudge of an unmasked axis is the identity.
+__device__ __forceinline__ bool ray_needs_careful_step(F3 src, F3 dir) {
+    const bool neg0 = (__float_as_uint(src.x) == 0x80000000u) | (__float_as_uint(src.y) == 0x80000000u) |
+                      (__float_as_uint(src.z) == 0x80000000u);
+    return neg0 || !(fminf(fminf(fabsf(dir.x), fabsf(dir.y)), fabsf(dir.z)) >= 0x1p-126f);
 }
 
 // Exact distance of a leaf voxel whose byte is 255 (distance >= 255): binary
@@ -147,10 +151,10 @@ __device__ __noinline__ uint32_t leaf_overflow(const DevGrid &g, uint32_t key) {
 
 // One loop iteration of hdda_ray. Returns 0xFF while the march continues,
 // otherwise the final state (0 hit, 1 out of bounds, 2 step cap); on return
-// r.i is the iteration count the shader reports. kNaN selects the NaN-aware
-// min/argmin (see ray_needs_nan_checks); both variants give identical results
-// on rays where tMax is never NaN.
-template <bool kNaN>
+// r.i is the iteration count the shader reports. kCareful selects the
+// NaN-aware min/argmin and the literal nudge (see ray_needs_careful_step);
+// both variants give identical results on the rays the fast one is used for.
+template <bool kCareful>
 __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     if (r.i >= kMaxSteps) return 2u;
     // vec3<i32>(floor(p)): one saturating round-down conversion (NaN -> 0).
@@ -163,15 +167,29 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     else if (r.np >= 1 && d < 4096u) lvl = 5;
     else lvl = 0;
     uint32_t dist = 1;
-    if (lvl == 0) {  // get_vdb_leaf_from_nothing (:398-413): linear scan of the N5 origins
-        const int kx = x & ~4095, ky = y & ~4095, kz = z & ~4095;
+    if (lvl == 0) {  // get_vdb_leaf_from_nothing (:398-413): the N5 whose origin is floor(p) & ~4095
         r.np = 0;
-        for (uint32_t k = 0; k < g.n5; k++) {
-            const int4 o = __ldg(&g.o5[k]);
-            if (o.x == kx && o.y == ky && o.z == kz) {
-                r.i5 = k;
-                lvl = 5;
-                break;
+        const int4 h0 = __ldg(g.root), h1 = __ldg(g.root + 1);
+        if (h1.w) {  // dense table of root keys (the first matching origin of the scan)
+            const uint32_t ux = (uint32_t)((x >> 12) - h0.x), uy = (uint32_t)((y >> 12) - h0.y),
+                           uz = (uint32_t)((z >> 12) - h0.z);
+            if (ux < (uint32_t)h0.w && uy < (uint32_t)h1.x && uz < (uint32_t)h1.y) {
+                const uint32_t *tab = reinterpret_cast<const uint32_t *>(g.root + 2 + g.n5);
+                const uint32_t e = __ldg(tab + (uz * (uint32_t)h1.x + uy) * (uint32_t)h0.w + ux);
+                if (e) {
+                    r.i5 = e - 1u;
+                    lvl = 5;
+                }
+            }
+        } else {  // linear scan, as the shader
+            const int kx = x & ~4095, ky = y & ~4095, kz = z & ~4095;
+            for (uint32_t k = 0; k < g.n5; k++) {
+                const int4 o = __ldg(g.root + 2 + k);
+                if (o.x == kx && o.y == ky && o.z == kz) {
+                    r.i5 = k;
+                    lvl = 5;
+                    break;
+                }
             }
         }
     }
@@ -214,25 +232,29 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     const float size = __uint2float_rn(dist) * __int_as_float((127 + sk) << 23);
     bool fast;
     const float ys = rcp_size(dist, sk, &fast);
-    float qx, qy, qz;
+    // tMax = idir * (size * step01 - (p - size * floor(p / size)))  (:78-80, :114)
+    float tx, ty, tz;
     // The fast quotient needs every coordinate of magnitude >= 2^-64 (a zero
     // coordinate also takes the IEEE path here; both give the same floor).
     if (fast && fminf(fminf(apx, apy), apz) >= 0x1p-64f) {
-        qx = div_fast(r.px, size, ys);
-        qy = div_fast(r.py, size, ys);
-        qz = div_fast(r.pz, size, ys);
+        // Here both products are exact, so each subtraction of a product is
+        // one FMA with the same rounding: size * step01 is 0 or size, and
+        // size * floor(p / size) = dist * f * 2^sk with |dist * f| <=
+        // 4096 / 2^sk + dist < 2^24 (|p| <= 4096 past the bounds test).
+        const float fx = floorf(div_fast(r.px, size, ys));
+        const float fy = floorf(div_fast(r.py, size, ys));
+        const float fz = floorf(div_fast(r.pz, size, ys));
+        tx = r.ix * __fmaf_rn(size, r.ax, -__fmaf_rn(-size, fx, r.px));
+        ty = r.iy * __fmaf_rn(size, r.ay, -__fmaf_rn(-size, fy, r.py));
+        tz = r.iz * __fmaf_rn(size, r.az, -__fmaf_rn(-size, fz, r.pz));
     } else {
-        qx = __fdiv_rn(r.px, size);
-        qy = __fdiv_rn(r.py, size);
-        qz = __fdiv_rn(r.pz, size);
+        tx = r.ix * (size * r.ax - (r.px - size * floorf(__fdiv_rn(r.px, size))));
+        ty = r.iy * (size * r.ay - (r.py - size * floorf(__fdiv_rn(r.py, size))));
+        tz = r.iz * (size * r.az - (r.pz - size * floorf(__fdiv_rn(r.pz, size))));
     }
-    // tMax = idir * (size * step01 - (p - size * floor(p / size)))  (:78-80, :114)
-    const float tx = r.ix * (size * r.ax - (r.px - size * floorf(qx)));
-    const float ty = r.iy * (size * r.ay - (r.py - size * floorf(qy)));
-    const float tz = r.iz * (size * r.az - (r.pz - size * floorf(qz)));
     float t;
     bool mx, my, mz;
-    if (kNaN) {
+    if (kCareful) {
         t = pmin(pmin(tx, ty), tz);
         mx = (tx <= ty) && (tx <= tz);
         my = (ty <= tz) && (ty <= tx);
@@ -252,10 +274,17 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     r.mx = mx;
     r.my = my;
     r.mz = mz;
-    // p += (4e-4 * step) * f32(mask)  (:122)
-    r.px = r.px + r.nx * (mx ? 1.0f : 0.0f);
-    r.py = r.py + r.ny * (my ? 1.0f : 0.0f);
-    r.pz = r.pz + r.nz * (mz ? 1.0f : 0.0f);
+    // p += (4e-4 * step) * f32(mask)  (:122); without a -0 coordinate the
+    // unmasked axes are unchanged.
+    if (kCareful) {
+        r.px = r.px + r.nx * (mx ? 1.0f : 0.0f);
+        r.py = r.py + r.ny * (my ? 1.0f : 0.0f);
+        r.pz = r.pz + r.nz * (mz ? 1.0f : 0.0f);
+    } else {
+        r.px = mx ? r.px + r.nx : r.px;
+        r.py = my ? r.py + r.ny : r.py;
+        r.pz = mz ? r.pz + r.nz : r.pz;
+    }
     r.i++;
     return 0xFFu;
 }
@@ -278,7 +307,7 @@ __device__ __forceinline__ March hdda(const DevGrid &g, F3 src, F3 dir) {
     Ray r;
     ray_init(r, src, dir);
     uint32_t st;
-    if (ray_needs_nan_checks(dir)) {
+    if (ray_needs_careful_step(src, dir)) {
         while ((st = ray_step<true>(g, r)) == 0xFFu) {
         }
     } else {

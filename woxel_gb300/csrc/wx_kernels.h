@@ -11,7 +11,7 @@ namespace wxk {
 
 // Device node pools of one grid (see api.cpp for the layout).
 struct DevGrid {
-    const int4 *o5;          // N5 origins
+    const int4 *root;        // root block: header, N5 origins, dense root-key table (api.cpp)
     const uint32_t *slot5;   // N5 slot words
     const uint32_t *slot4;   // N4 slot words
     const uint8_t *leaf;     // N3: one byte per voxel, 0 hit, 1..254 distance, 255 = see ovf
