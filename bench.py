@@ -45,10 +45,44 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
+def l2_copy_peak(dev, mib: int = 32, reps: int = 300) -> float:
+    """L2 bandwidth measured here: GB/s of back-to-back device copies between two buffers
+    that together fit in L2 (2 x 32 MiB of the 129 MB)."""
+    import torch
+
+    a = torch.ones(mib << 18, dtype=torch.float32, device=dev)
+    b = torch.empty_like(a)
+    for _ in range(10):
+        b.copy_(a)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        b.copy_(a)
+    e1.record()
+    torch.cuda.synchronize()
+    return 2 * a.numel() * 4 * reps / (e0.elapsed_time(e1) / 1e3) / 1e9
+
+
+def max_over_ranks(ms: float, dist=None, device=None) -> float:
+    """The slowest rank's step time (every rank gets it); ms itself without a process group."""
+    if dist is None:
+        return ms
+    import torch
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(rays_per_rank: int, world: int, ms: float) -> float:
+    """Whole-job Grays/s of `world` replicas that each trace rays_per_rank rays in ms (weak scaling)."""
+    return world * rays_per_rank / (ms / 1e3) / 1e9
+
+
 def profiled_traffic(kernel: str, workload: str):
     """DRAM bytes (read + write) per launch from the committed ncu summary of this kernel and
-    workload (profiles/<kernel>_<workload>_1080p.md, line 'dram_bytes_per_launch: N'), else None."""
-    p = ROOT / "profiles" / f"{kernel}_{workload}_1080p.md"
+    workload (profiles/<kernel>_<workload>.md, line 'dram_bytes_per_launch: N'), else None."""
+    p = ROOT / "profiles" / f"{kernel}_{workload}.md"
     try:
         for line in p.read_text().splitlines():
             if line.strip().startswith("dram_bytes_per_launch:"):
@@ -447,13 +481,9 @@ def main():
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-    ms = statistics.mean(step_ms)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(statistics.mean(step_ms), dist, dev)
     rays_step = wl.rays
-    value = world * rays_step / (ms / 1e3) / 1e9
+    value = replica_throughput(rays_step, world, ms)
     lat = sorted(launch_ms)
     p50 = lat[len(lat) // 2]
     p99 = lat[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]
@@ -477,10 +507,23 @@ def main():
             step_host()
             torch.cuda.synchronize()
             e_ms.append(1e3 * (time.perf_counter() - t1))
-        em = statistics.mean(e_ms)
-        e2e = {"value": world * rays_step / (em / 1e3) / 1e9, "unit": "Grays/s",
+        em = max_over_ranks(statistics.mean(e_ms), dist, dev)
+        e2e = {"value": replica_throughput(rays_step, world, em), "unit": "Grays/s",
                "h2d_bytes_per_step": 256 * len(frames), "d2h_bytes_per_step": W_ * H_ * 4 * len(frames),
                "ms_per_step": em}
+
+    # Mode 3 traces one shadow ray per lit hit inside the same launches; they are not in `value`.
+    # Counted from the hit records of one untimed render of each frame.
+    shadow = None
+    if frames[0].mode == 3:
+        hb = torch.empty(W_ * H_ * 32, dtype=torch.uint8, device=dev)
+        n_sh = 0
+        for st, o in zip(states, outs):
+            ctx.render(grid, st, W_, H_, o, hb, stream=sh)
+            n_sh += int((hb.view(torch.int32).view(-1, 8)[:, 6] & 1).sum().item())
+        del hb
+        shadow = {"rays_per_step": n_sh, "value": world * n_sh / (ms / 1e3) / 1e9, "unit": "Grays/s",
+                  "note": "shadow rays traced in the timed launches, rate over the same time; not part of value"}
 
     # BASELINE config 4: batched vs plain on the mixed-resolution load (needs the 2000-sphere grid)
     batched = None
@@ -491,7 +534,7 @@ def main():
 
     # roofline + CPU baseline from the oracle on a sample of the same tiles (rank 0)
     roof, cpu = None, None
-    kernel_name = "k_persistent" if args.kernel == "persistent" else "k_pixel"
+    kernel_name = "k_persistent" if ctx.tuning["kernel"] == 0 else "k_pixel"  # after autotuning
     if rank == 0:
         peak, peak_kind = hbm_peak()
         view = topo.view()
@@ -500,14 +543,20 @@ def main():
         launch_avg_ms = statistics.mean(launch_ms)
         bytes_launch = bpr * frames[0].rays
         achieved = bytes_launch / (launch_avg_ms / 1e3) / 1e9
+        l2 = l2_copy_peak(dev)
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": profiled_traffic(kernel_name, args.workload), "peak_kind": peak_kind,
                 "kernel": kernel_name, "algorithmic_bytes_per_ray": bpr,
-                "algorithmic_bytes_per_launch": bytes_launch, "launch_ms": launch_avg_ms}
+                "algorithmic_bytes_per_launch": bytes_launch, "launch_ms": launch_avg_ms,
+                "l2": {"peak": l2, "frac": achieved / l2,
+                       "peak_kind": "measured here: device copy between two L2-resident 32 MiB buffers"}}
         if not args.no_cpu:
             cpu = {"value": rays_s / secs / 1e9, "unit": "Grays/s", "cores": nthreads, "kind": "port",
                    "sample": f"{args.cpu_fraction:.4f} of the 8x4 tiles of each of the {len(frames)} frames "
                              f"({rays_s} rays), C restatement of raycast.comp.wgsl, {nthreads} threads"}
+            r1, s1, _ = oracle_sample(view, frames, args.cpu_fraction / 16, 1, seed=6)
+            cpu["single_thread"] = {"value": r1 / s1 / 1e9, "unit": "Grays/s", "cores": 1,
+                                    "sample": f"{args.cpu_fraction / 16:.5f} of the tiles ({r1} rays)"}
         del view
 
     if rank == 0:
@@ -522,7 +571,7 @@ def main():
                        "autotune": tuned and {"table [kernel, tile_w, warps/block, ms for 4 frames]": tuned["table"],
                                               "seconds": tuned["seconds"]}},
             "frame_latency_ms": {"p50": p50, "p99": p99},
-            "batched": batched,
+            "batched": batched, "shadow_rays": shadow,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "gpu_launches": len(frames) * args.steps,
             "clocks": clk.summary(),
