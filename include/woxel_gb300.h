@@ -138,8 +138,20 @@ int wx_grid_upload(wx_ctx *ctx, const wx_vdb345_view *view, wx_grid **out);
 /* Native: compute the per-level SDF (vdb345.rs:290-670) on the host and pack
  * the pools directly from a topology, without the padded atlas. */
 int wx_grid_build(wx_ctx *ctx, wx_topology *topo, wx_grid **out);
+/* wx_grid_build with the SDF and the packing on the GPU (compute_sdf,
+ * vdb345.rs:290-670): the same device pools word for word. Needs N5 origins
+ * that are multiples of 4096 (else WX_ERR_UNSUPPORTED). Temporary device
+ * memory: about 4 bytes per leaf voxel plus 200 bytes per node. */
+int wx_grid_build_gpu(wx_ctx *ctx, const wx_topology *topo, wx_grid **out);
 int wx_grid_release(wx_ctx *ctx, wx_grid *grid);
 int wx_grid_get_info(const wx_grid *grid, wx_grid_info *out);
+/* Copies a grid's device pools to host memory; any pointer may be NULL.
+ * slot5: n5*32768 u32, slot4: n4*4096 u32 (bit 31 = child index, else the skip
+ * distance, 0 = hit), leaf: n3*512 bytes (0 hit, 1..254 distance, 255 = see
+ * ovf), ovf: *n_ovf pairs (leaf << 9 | voxel, distance) sorted by key.
+ * No reference counterpart. */
+int wx_grid_read_pools(wx_ctx *ctx, const wx_grid *grid, uint32_t *slot5, uint32_t *slot4, uint8_t *leaf,
+                       uint32_t *ovf, uint64_t *n_ovf);
 
 /* ---- the raycast pass: replaces cp_main (raycast.comp.wgsl:60-68) ---- */
 /* Renders the (8*floor(w/8)) x (4*floor(h/4)) pixels the reference dispatch

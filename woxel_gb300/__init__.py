@@ -214,6 +214,17 @@ class Grid:
         check(lib().wx_grid_get_info(self._h, C.byref(i)))
         return {k: int(getattr(i, k)) for k, _ in wx_grid_info._fields_}
 
+    def pools(self) -> dict:
+        """Copies of the device pools: slot5, slot4 (u32), leaf (u8) and ovf ((key, distance) u32 pairs)."""
+        i = self.info
+        n = C.c_uint64()
+        check(lib().wx_grid_read_pools(self.ctx._h, self._h, None, None, None, None, C.byref(n)), self.ctx._h)
+        out = {"slot5": np.empty(i["n5"] * 32768, np.uint32), "slot4": np.empty(i["n4"] * 4096, np.uint32),
+               "leaf": np.empty(i["n3"] * 512, np.uint8), "ovf": np.empty((n.value, 2), np.uint32)}
+        check(lib().wx_grid_read_pools(self.ctx._h, self._h, out["slot5"].ctypes.data, out["slot4"].ctypes.data,
+                                       out["leaf"].ctypes.data, out["ovf"].ctypes.data, C.byref(n)), self.ctx._h)
+        return out
+
     def release(self) -> None:
         if self._h and self._h.value:
             check(lib().wx_grid_release(self.ctx._h, self._h), self.ctx._h)
@@ -244,9 +255,12 @@ class Context:
         except Exception:
             pass
 
-    def build_grid(self, topo: Topology) -> Grid:
+    def build_grid(self, topo: Topology, gpu: bool = False) -> Grid:
+        """Compute the SDF and pack the device pools from a topology: on the host
+        (wx_grid_build) or on the GPU (wx_grid_build_gpu); both give the same pools."""
         out = C.c_void_p()
-        check(lib().wx_grid_build(self._h, topo._h, C.byref(out)), self._h)
+        fn = lib().wx_grid_build_gpu if gpu else lib().wx_grid_build
+        check(fn(self._h, topo._h, C.byref(out)), self._h)
         return Grid(self, out.value)
 
     def upload_view(self, v: dict) -> Grid:

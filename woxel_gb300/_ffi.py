@@ -89,6 +89,8 @@ SIGNATURES = {
     "wx_last_error": (C.c_char_p, [P]),
     "wx_grid_upload": (INT, [P, C.POINTER(wx_vdb345_view), C.POINTER(P)]),
     "wx_grid_build": (INT, [P, P, C.POINTER(P)]),
+    "wx_grid_build_gpu": (INT, [P, P, C.POINTER(P)]),
+    "wx_grid_read_pools": (INT, [P, P, P, P, P, P, C.POINTER(C.c_uint64)]),
     "wx_grid_release": (INT, [P, P]),
     "wx_grid_get_info": (INT, [P, C.POINTER(wx_grid_info)]),
     "wx_render": (INT, [P, P, C.POINTER(wx_state_uniform), U32, U32, P, P, P]),

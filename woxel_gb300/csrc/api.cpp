@@ -101,6 +101,21 @@ bool device_accessible(const void *p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// A device allocation freed on scope exit (temporaries of wx_grid_build_gpu).
+struct DevBuf {
+    void *p = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    template <class T>
+    T *as() const {
+        return static_cast<T *>(p);
+    }
+};
+
 template <class F>
 void parallel_chunks(size_t n, F f) {
     unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -159,14 +174,71 @@ std::vector<int4> root_block(const std::vector<int4> &o5, uint64_t n5) {
     return b;
 }
 
+// The kernels address each pool with a 32-bit element index (node << log2 slots | slot).
+int check_pool_limits(wx_ctx *ctx, uint64_t n5, uint64_t n4, uint64_t n3) {
+    if (n5 > (1u << 17) || n4 > (1u << 20) || n3 > (1u << 23))
+        return fail(ctx, WX_ERR_UNSUPPORTED,
+                    "grid too large: at most 131072 N5, 1048576 N4 and 8388608 N3 nodes");
+    return WX_OK;
+}
+
+// One device block for all pools of a grid (layout at the top of this file);
+// the root block is copied in, the other pools are left for the caller.
+int alloc_grid(wx_ctx *ctx, const std::vector<int4> &o5, uint64_t n5, uint64_t n4, uint64_t n3, uint64_t n_ovf,
+               wx_grid **out) {
+    auto *gr = new (std::nothrow) wx_grid();
+    if (!gr) return fail(ctx, WX_ERR_OOM, "host allocation failed");
+    std::vector<int4> root;
+    try {
+        root = root_block(o5, n5);
+    } catch (...) {
+        delete gr;
+        return fail(ctx, WX_ERR_OOM, "host allocation failed");
+    }
+    auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t b_o5 = align(root.size() * 16), b5 = align(n5 * 32768ull * 4),
+                 b4 = align(n4 * 4096ull * 4), b3 = align(n3 * 512ull), bo = align(n_ovf * 8);
+    gr->bytes = b_o5 + b5 + b4 + b3 + bo;
+    gr->device = ctx->device;
+    cudaError_t e = cudaMalloc(&gr->dev, gr->bytes);
+    if (e != cudaSuccess) {
+        delete gr;
+        return cuda_fail(ctx, e, "cudaMalloc(node pools)");
+    }
+    char *b = static_cast<char *>(gr->dev);
+    gr->g.root = reinterpret_cast<const int4 *>(b);
+    gr->g.slot5 = reinterpret_cast<const uint32_t *>(b + b_o5);
+    gr->g.slot4 = reinterpret_cast<const uint32_t *>(b + b_o5 + b5);
+    gr->g.leaf = reinterpret_cast<const uint8_t *>(b + b_o5 + b5 + b4);
+    gr->g.ovf = reinterpret_cast<const uint2 *>(b + b_o5 + b5 + b4 + b3);
+    gr->g.n5 = (uint32_t)n5;
+    gr->g.n_ovf = (uint32_t)n_ovf;
+    gr->info.n5 = n5;
+    gr->info.n4 = n4;
+    gr->info.n3 = n3;
+    gr->info.device_bytes = gr->bytes;
+    e = cudaMemcpy((void *)gr->g.root, root.data(), root.size() * 16, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(gr->dev);
+        delete gr;
+        return cuda_fail(ctx, e, "cudaMemcpy(root block)");
+    }
+    *out = gr;
+    return WX_OK;
+}
+
+void free_grid(wx_grid *gr) {
+    if (!gr) return;
+    cudaFree(gr->dev);
+    delete gr;
+}
+
 // Pack the per-voxel u32 leaf distances into bytes plus the overflow table,
 // allocate one device block for all pools and upload them.
 int upload_pools(wx_ctx *ctx, const std::vector<int4> &o5, const uint32_t *s5, const uint32_t *s4, const uint32_t *s3,
                  uint64_t n5, uint64_t n4, uint64_t n3, wx_grid **out) {
-    // The kernels address each pool with a 32-bit element index (node << log2 slots | slot).
-    if (n5 > (1u << 17) || n4 > (1u << 20) || n3 > (1u << 23))
-        return fail(ctx, WX_ERR_UNSUPPORTED,
-                    "grid too large: at most 131072 N5, 1048576 N4 and 8388608 N3 nodes");
+    int rc = check_pool_limits(ctx, n5, n4, n3);
+    if (rc != WX_OK) return rc;
     std::vector<uint8_t> leaf;
     std::vector<uint2> ovf;
     try {
@@ -190,46 +262,16 @@ int upload_pools(wx_ctx *ctx, const std::vector<int4> &o5, const uint32_t *s5, c
     } catch (...) {
         return fail(ctx, WX_ERR_OOM, "host allocation failed while packing leaves");
     }
-    auto *gr = new (std::nothrow) wx_grid();
-    if (!gr) return fail(ctx, WX_ERR_OOM, "host allocation failed");
-    std::vector<int4> root;
-    try {
-        root = root_block(o5, n5);
-    } catch (...) {
-        delete gr;
-        return fail(ctx, WX_ERR_OOM, "host allocation failed");
-    }
-    auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    const size_t b_o5 = align(root.size() * 16), b5 = align(n5 * 32768ull * 4),
-                 b4 = align(n4 * 4096ull * 4), b3 = align(n3 * 512ull), bo = align(ovf.size() * 8);
-    gr->bytes = b_o5 + b5 + b4 + b3 + bo;
-    gr->device = ctx->device;
-    cudaError_t e = cudaMalloc(&gr->dev, gr->bytes);
-    if (e != cudaSuccess) {
-        delete gr;
-        return cuda_fail(ctx, e, "cudaMalloc(node pools)");
-    }
-    char *b = static_cast<char *>(gr->dev);
-    gr->g.root = reinterpret_cast<const int4 *>(b);
-    gr->g.slot5 = reinterpret_cast<const uint32_t *>(b + b_o5);
-    gr->g.slot4 = reinterpret_cast<const uint32_t *>(b + b_o5 + b5);
-    gr->g.leaf = reinterpret_cast<const uint8_t *>(b + b_o5 + b5 + b4);
-    gr->g.ovf = reinterpret_cast<const uint2 *>(b + b_o5 + b5 + b4 + b3);
-    gr->g.n5 = (uint32_t)n5;
-    gr->g.n_ovf = (uint32_t)ovf.size();
-    gr->info.n5 = n5;
-    gr->info.n4 = n4;
-    gr->info.n3 = n3;
-    gr->info.device_bytes = gr->bytes;
-    if (e == cudaSuccess) e = cudaMemcpy((void *)gr->g.root, root.data(), root.size() * 16, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && n5) e = cudaMemcpy((void *)gr->g.slot5, s5, n5 * 32768ull * 4, cudaMemcpyHostToDevice);
+    wx_grid *gr = nullptr;
+    if ((rc = alloc_grid(ctx, o5, n5, n4, n3, ovf.size(), &gr)) != WX_OK) return rc;
+    cudaError_t e = cudaSuccess;
+    if (n5) e = cudaMemcpy((void *)gr->g.slot5, s5, n5 * 32768ull * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && n4) e = cudaMemcpy((void *)gr->g.slot4, s4, n4 * 4096ull * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && n3) e = cudaMemcpy((void *)gr->g.leaf, leaf.data(), leaf.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !ovf.empty())
         e = cudaMemcpy((void *)gr->g.ovf, ovf.data(), ovf.size() * 8, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
-        cudaFree(gr->dev);
-        delete gr;
+        free_grid(gr);
         return cuda_fail(ctx, e, "cudaMemcpy(node pools)");
     }
     *out = gr;
@@ -478,6 +520,159 @@ int wx_grid_build(wx_ctx *ctx, wx_topology *t, wx_grid **out) {
     if (rc != WX_OK) return rc;
     gr->info.active_voxels = wx_topology_active_voxels(t);
     *out = gr;
+    return WX_OK;
+}
+
+// The same pools as wx_grid_build, with compute_sdf and the packing on the
+// GPU (sdf.cu). The host uploads only the masks, the N5 origins and per-word
+// child-count prefixes; child tables, child origins, neighbour tables, the
+// three sweeps and the packing run on the device.
+int wx_grid_build_gpu(wx_ctx *ctx, const wx_topology *t, wx_grid **out) {
+    if (!ctx || !t || !out) return fail(ctx, WX_ERR_INVALID, "wx_grid_build_gpu: null argument");
+    WX_CUDA(ctx, cudaSetDevice(ctx->device));
+    using namespace wx;
+    const uint64_t n5 = t->n5(), n4 = t->n4(), n3 = t->n3();
+    int rc = check_pool_limits(ctx, n5, n4, n3);
+    if (rc != WX_OK) return rc;
+    if (t->kid5.size() != n5 * kN5Words || t->val5.size() != n5 * kN5Words || t->kid4.size() != n4 * kN4Words ||
+        t->val4.size() != n4 * kN4Words || t->val3.size() != n3 * kN3Words || t->first4.size() != n5 ||
+        t->first3.size() != n4)
+        return fail(ctx, WX_ERR_INVALID, "wx_grid_build_gpu: masks and node counts disagree");
+    std::vector<int4> o5(std::max<uint64_t>(n5, 1));
+    std::vector<uint32_t> pre5, pre4;
+    try {
+        pre5.resize(n5 * kN5Words);
+        pre4.resize(n4 * kN4Words);
+    } catch (...) {
+        return fail(ctx, WX_ERR_OOM, "wx_grid_build_gpu: host allocation failed");
+    }
+    for (uint64_t i = 0; i < n5; i++) {
+        o5[i] = make_int4(t->o5[i][0], t->o5[i][1], t->o5[i][2], 0);
+        if ((o5[i].x & 4095) || (o5[i].y & 4095) || (o5[i].z & 4095))
+            return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_build_gpu: N5 origins must be multiples of 4096");
+    }
+    auto prefix = [](const std::vector<uint64_t> &kid, uint64_t nodes, uint32_t words, std::vector<uint32_t> &pre) {
+        for (uint64_t n = 0; n < nodes; n++) {
+            uint32_t acc = 0;
+            for (uint32_t w = 0; w < words; w++) {
+                pre[n * words + w] = acc;
+                acc += (uint32_t)__builtin_popcountll(kid[n * words + w]);
+            }
+        }
+    };
+    prefix(t->kid5, n5, kN5Words, pre5);
+    prefix(t->kid4, n4, kN4Words, pre4);
+    std::vector<int4> root;
+    try {
+        root = root_block(o5, n5);
+    } catch (...) {
+        return fail(ctx, WX_ERR_OOM, "wx_grid_build_gpu: host allocation failed");
+    }
+
+    const uint64_t nmax = std::max<uint64_t>({n5, n4, n3, 1});
+    DevBuf kid5, val5, kid4, val4, val3, dpre5, dpre4, first4, first3, droot, c5, c4, org5, org4, org3, d5, d4, d3,
+        nb, indeg, queue, ctr;
+    struct Alloc {
+        DevBuf *b;
+        size_t bytes;
+    } allocs[] = {{&kid5, n5 * kN5Words * 8},  {&val5, n5 * kN5Words * 8}, {&kid4, n4 * kN4Words * 8},
+                  {&val4, n4 * kN4Words * 8},  {&val3, n3 * kN3Words * 8}, {&dpre5, n5 * kN5Words * 4},
+                  {&dpre4, n4 * kN4Words * 4}, {&first4, n5 * 4},          {&first3, n4 * 4},
+                  {&droot, root.size() * 16},  {&c5, n5 * kN5Slots * 4},   {&c4, n4 * kN4Slots * 4},
+                  {&org5, n5 * 16},            {&org4, n4 * 16},           {&org3, n3 * 16},
+                  {&d5, n5 * kN5Slots * 4},    {&d4, n4 * kN4Slots * 4},   {&d3, n3 * kN3Slots * 4},
+                  {&nb, nmax * 27 * 4},        {&indeg, nmax * 4},         {&queue, nmax * 4},
+                  {&ctr, 8 * 4}};
+    for (auto &a : allocs)
+        if (a.bytes) WX_CUDA(ctx, cudaMalloc(&a.b->p, a.bytes));
+    struct Up {
+        DevBuf *b;
+        const void *src;
+        size_t bytes;
+    } ups[] = {{&kid5, t->kid5.data(), n5 * kN5Words * 8}, {&val5, t->val5.data(), n5 * kN5Words * 8},
+               {&kid4, t->kid4.data(), n4 * kN4Words * 8}, {&val4, t->val4.data(), n4 * kN4Words * 8},
+               {&val3, t->val3.data(), n3 * kN3Words * 8}, {&dpre5, pre5.data(), n5 * kN5Words * 4},
+               {&dpre4, pre4.data(), n4 * kN4Words * 4},   {&first4, t->first4.data(), n5 * 4},
+               {&first3, t->first3.data(), n4 * 4},        {&droot, root.data(), root.size() * 16},
+               {&org5, o5.data(), n5 * 16}};
+    for (auto &u : ups)
+        if (u.bytes) WX_CUDA(ctx, cudaMemcpy(u.b->p, u.src, u.bytes, cudaMemcpyHostToDevice));
+    const cudaStream_t st = nullptr;
+    WX_CUDA(ctx, cudaMemsetAsync(ctr.p, 0, 8 * 4, st));
+    WX_CUDA(ctx, wxk::sdf_child_table(kid5.as<uint64_t>(), dpre5.as<uint32_t>(), first4.as<uint32_t>(), n5, 15,
+                                      c5.as<uint32_t>(), st));
+    WX_CUDA(ctx, wxk::sdf_child_table(kid4.as<uint64_t>(), dpre4.as<uint32_t>(), first3.as<uint32_t>(), n4, 12,
+                                      c4.as<uint32_t>(), st));
+    WX_CUDA(ctx, wxk::sdf_child_origins(c5.as<uint32_t>(), org5.as<int4>(), n5, 5, 7, org4.as<int4>(), st));
+    WX_CUDA(ctx, wxk::sdf_child_origins(c4.as<uint32_t>(), org4.as<int4>(), n4, 4, 3, org3.as<int4>(), st));
+    WX_CUDA(ctx, wxk::sdf_init(kid5.as<uint64_t>(), n5 * kN5Slots, d5.as<uint32_t>(), st));
+    WX_CUDA(ctx, wxk::sdf_init(kid4.as<uint64_t>(), n4 * kN4Slots, d4.as<uint32_t>(), st));
+    WX_CUDA(ctx, wxk::sdf_init(val3.as<uint64_t>(), n3 * kN3Slots, d3.as<uint32_t>(), st));
+    const wxk::SdfTree tree{droot.as<int4>(), (uint32_t)n5, c5.as<uint32_t>(), c4.as<uint32_t>()};
+    struct Level {
+        int L;
+        DevBuf *org, *d;
+        uint64_t nc;
+    } levels[] = {{5, &org5, &d5, n5}, {4, &org4, &d4, n4}, {3, &org3, &d3, n3}};
+    for (auto &lv : levels) {
+        WX_CUDA(ctx, wxk::sdf_neighbours(lv.L, lv.org->as<int4>(), (uint32_t)lv.nc, tree, nb.as<uint32_t>(), st));
+        WX_CUDA(ctx, wxk::sdf_sweep(lv.L, lv.d->as<uint32_t>(), nb.as<uint32_t>(), (uint32_t)lv.nc,
+                                    indeg.as<uint32_t>(), queue.as<uint32_t>(), ctr.as<uint32_t>(), ctx->num_sms, st));
+    }
+    // Count the leaf overflow entries (ctr[3]) to size the grid block.
+    uint32_t *flags = ctr.as<uint32_t>();
+    WX_CUDA(ctx, wxk::sdf_pack_leaves(d3.as<uint32_t>(), n3 * kN3Slots, nullptr, nullptr, 0, flags + 3, st));
+    uint32_t h[8];
+    WX_CUDA(ctx, cudaMemcpy(h, flags, sizeof h, cudaMemcpyDeviceToHost));
+    if (h[2]) return fail(ctx, WX_ERR_CUDA, "wx_grid_build_gpu: a sweep's dependency wait hit its bound");
+    const uint64_t n_ovf = h[3];
+    wx_grid *gr = nullptr;
+    if ((rc = alloc_grid(ctx, o5, n5, n4, n3, n_ovf, &gr)) != WX_OK) return rc;
+    cudaError_t e = cudaMemsetAsync(flags + 3, 0, 2 * 4, st);  // ctr[3] overflow count, ctr[4] distance error
+    if (e == cudaSuccess)
+        e = wxk::sdf_pack_internal(kid5.as<uint64_t>(), val5.as<uint64_t>(), c5.as<uint32_t>(), d5.as<uint32_t>(),
+                                   n5 * kN5Slots, const_cast<uint32_t *>(gr->g.slot5), flags + 4, st);
+    if (e == cudaSuccess)
+        e = wxk::sdf_pack_internal(kid4.as<uint64_t>(), val4.as<uint64_t>(), c4.as<uint32_t>(), d4.as<uint32_t>(),
+                                   n4 * kN4Slots, const_cast<uint32_t *>(gr->g.slot4), flags + 4, st);
+    if (e == cudaSuccess)
+        e = wxk::sdf_pack_leaves(d3.as<uint32_t>(), n3 * kN3Slots, const_cast<uint8_t *>(gr->g.leaf),
+                                 const_cast<uint2 *>(gr->g.ovf), (uint32_t)n_ovf, flags + 3, st);
+    if (e == cudaSuccess) e = cudaMemcpy(h, flags, sizeof h, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        free_grid(gr);
+        return cuda_fail(ctx, e, "wx_grid_build_gpu: packing");
+    }
+    if (h[4]) {
+        free_grid(gr);
+        return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_build_gpu: tile distance >= 2^31");
+    }
+    if (n_ovf) {  // entries arrive in any order; the kernels binary-search them by key
+        std::vector<uint2> ov(n_ovf);
+        e = cudaMemcpy(ov.data(), gr->g.ovf, n_ovf * 8, cudaMemcpyDeviceToHost);
+        std::sort(ov.begin(), ov.end(), [](const uint2 &a, const uint2 &b) { return a.x < b.x; });
+        if (e == cudaSuccess) e = cudaMemcpy((void *)gr->g.ovf, ov.data(), n_ovf * 8, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            free_grid(gr);
+            return cuda_fail(ctx, e, "wx_grid_build_gpu: overflow table");
+        }
+    }
+    gr->info.active_voxels = wx_topology_active_voxels(t);
+    *out = gr;
+    return WX_OK;
+}
+
+int wx_grid_read_pools(wx_ctx *ctx, const wx_grid *grid, uint32_t *slot5, uint32_t *slot4, uint8_t *leaf,
+                       uint32_t *ovf, uint64_t *n_ovf) {
+    if (!ctx || !grid) return fail(ctx, WX_ERR_INVALID, "wx_grid_read_pools: null argument");
+    WX_CUDA(ctx, cudaSetDevice(grid->device));
+    if (n_ovf) *n_ovf = grid->g.n_ovf;
+    const uint64_t n5 = grid->info.n5, n4 = grid->info.n4, n3 = grid->info.n3;
+    if (slot5 && n5) WX_CUDA(ctx, cudaMemcpy(slot5, grid->g.slot5, n5 * wx::kN5Slots * 4, cudaMemcpyDeviceToHost));
+    if (slot4 && n4) WX_CUDA(ctx, cudaMemcpy(slot4, grid->g.slot4, n4 * wx::kN4Slots * 4, cudaMemcpyDeviceToHost));
+    if (leaf && n3) WX_CUDA(ctx, cudaMemcpy(leaf, grid->g.leaf, n3 * wx::kN3Slots, cudaMemcpyDeviceToHost));
+    if (ovf && grid->g.n_ovf)
+        WX_CUDA(ctx, cudaMemcpy(ovf, grid->g.ovf, (size_t)grid->g.n_ovf * 8, cudaMemcpyDeviceToHost));
     return WX_OK;
 }
 

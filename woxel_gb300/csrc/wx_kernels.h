@@ -50,8 +50,30 @@ bool grid_device_view(const wx_grid *grid, DevGrid *out, int *device);
 // Device index and SM count of a context (defined in api.cpp).
 void ctx_device_info(const wx_ctx *ctx, int *device, int *num_sms);
 
+// GPU SDF build (sdf.cu). The tree structure the sweeps look neighbours up in:
+// the root block of the grid layout (header, origins, root-key table) and the
+// child-index tables (slot -> child DFS index or 0xFFFFFFFF).
+struct SdfTree {
+    const int4 *root;
+    uint32_t n5;
+    const uint32_t *c5, *c4;
+};
+cudaError_t sdf_child_table(const uint64_t *kid, const uint32_t *pre, const uint32_t *first, uint64_t nodes,
+                            int slots_log2, uint32_t *cidx, cudaStream_t st);
+cudaError_t sdf_child_origins(const uint32_t *cidx, const int4 *org, uint64_t nodes, int log2d, int child_span_log2,
+                              int4 *org_child, cudaStream_t st);
+cudaError_t sdf_init(const uint64_t *solid, uint64_t ncells, uint32_t *d, cudaStream_t st);
+cudaError_t sdf_neighbours(int level, const int4 *org, uint32_t nc, const SdfTree &t, uint32_t *nb, cudaStream_t st);
+// Both passes of one level; ctr[2] (not reset here) is set when a wait hit its bound.
+cudaError_t sdf_sweep(int level, uint32_t *d, const uint32_t *nb, uint32_t nc, uint32_t *indeg, uint32_t *queue,
+                      uint32_t *ctr, int num_sms, cudaStream_t st);
+cudaError_t sdf_pack_internal(const uint64_t *kid, const uint64_t *val, const uint32_t *cidx, const uint32_t *d,
+                              uint64_t nslots, uint32_t *slot, uint32_t *err, cudaStream_t st);
+cudaError_t sdf_pack_leaves(const uint32_t *d, uint64_t ncells, uint8_t *leaf, uint2 *ovf, uint32_t cap,
+                            uint32_t *n_ovf, cudaStream_t st);
+
 // Exhaustive check of the fast floor-division path against IEEE division:
-// every odd m < max_m and every significand of [1,2) and [-2,-1).
+// every divisor m < max_m and every significand of [1,2) and [-2,-1).
 // out[0] = mismatch count, out[1] = first mismatching m, out[2] = its x bits.
 cudaError_t check_division(uint32_t max_m, unsigned long long *out_dev, cudaStream_t st);
 
