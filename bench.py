@@ -435,7 +435,13 @@ def main():
     grid = ctx.build_grid(topo)
     t_build = time.perf_counter() - t0
     info = grid.info
-    log(f"[bench] grid {args.workload}: {info} gen {t_gen:.1f}s sdf+upload {t_build:.1f}s")
+    # The same pools built on the GPU (wx_grid_build_gpu), timed for the record and released.
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    ctx.build_grid(topo, gpu=True).release()
+    torch.cuda.synchronize(dev)
+    t_build_gpu = time.perf_counter() - t0
+    log(f"[bench] grid {args.workload}: {info} gen {t_gen:.1f}s sdf+upload {t_build:.1f}s (gpu {t_build_gpu:.2f}s)")
     frames = wl.frames
     states = [f.state() for f in frames]
     W_, H_ = frames[0].width, frames[0].height
@@ -566,6 +572,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"{args.workload}: {len(frames)} x {W_}x{H_} frames, plain per-frame launches",
                        "grid": {k: info[k] for k in ("n5", "n4", "n3", "active_voxels", "device_bytes")},
+                       "grid_build_s": {"host_sdf": round(t_build, 3), "gpu_sdf": round(t_build_gpu, 3)},
                        "render_mode": frames[0].mode, "l2": "flushed between steps (512 MB write)",
                        "parallelism": f"replicas x{world}", "tuning": ctx.tuning,
                        "autotune": tuned and {"table [kernel, tile_w, warps/block, ms for 4 frames]": tuned["table"],
