@@ -65,6 +65,27 @@ def test_spheres_batched_equals_plain_and_repeatable(cuda_ctx, spheres):
         np.testing.assert_array_equal(o.cpu().numpy().reshape(f.height, f.width, 4), a)
 
 
+@pytest.mark.parametrize("mode", [3, 0])
+def test_spheres_all_kernels_agree(cuda_ctx, spheres, mode):
+    """Whole 1080p frames: the per-tile kernel and other tile shapes write the same RGBA8 and
+    hit records as the tile-queue kernel, bit for bit."""
+    _, _, grid = spheres
+    before = cuda_ctx.tuning
+    try:
+        for f in W.spheres_frames()[:4]:
+            st = f.state()
+            st.render_mode[0] = mode
+            outs = []
+            for k, tw in ((0, 8), (1, 4), (0, 16), (1, 32)):
+                cuda_ctx.set_tuning(kernel=k, tile_width=tw)
+                outs.append(gpu_render(cuda_ctx, grid, st, f.width, f.height))
+            for rg, hg in outs[1:]:
+                np.testing.assert_array_equal(rg, outs[0][0])
+                np.testing.assert_array_equal(hg.view(np.uint8), outs[0][1].view(np.uint8))
+    finally:
+        cuda_ctx.set_tuning(**before)
+
+
 def test_noise_4k_sampled_tiles(cuda_ctx):
     topo = W.noise_topology()
     n5, n4, n3 = topo.counts

@@ -21,8 +21,9 @@ namespace wxd {
 constexpr uint32_t kChild = 0x80000000u;
 constexpr uint32_t kMaxSteps = 1000u;  // HDDA_MAX_RAY_STEPS, raycast.comp.wgsl:82
 
-// o5: N5 origins in DFS order; slot5/slot4: n5*32768 and n4*4096 slot words;
-// leaf: n3*512 voxel bytes (0 hit, 1..254 distance, 255 = exact distance in ovf).
+// root: header, N5 origins in DFS order and the dense root-key table;
+// slot5/slot4: n5*32768 and n4*4096 slot words; leaf: n3*512 voxel bytes
+// (0 hit, 1..254 distance, 255 = exact distance in ovf).
 using DevGrid = wxk::DevGrid;
 
 // RN(1 / d) for 1 <= d < kRcp (entry 0 unused): filled once per device from
@@ -302,6 +303,18 @@ struct March {
     uint32_t mask;   // bit0 x, bit1 y, bit2 z
 };
 
+// HDDAout of a ray that returned state st (raycast.comp.wgsl:128-142).
+__device__ __forceinline__ March march_result(const Ray &r, uint32_t st) {
+    March m;
+    m.p = f3(r.px, r.py, r.pz);
+    m.state = st;
+    m.np = r.np;
+    m.node = ray_node(r);
+    m.i = r.i;
+    m.mask = ray_mask(r);
+    return m;
+}
+
 // hdda_ray (raycast.comp.wgsl:84-126) run to completion.
 __device__ __forceinline__ March hdda(const DevGrid &g, F3 src, F3 dir) {
     Ray r;
@@ -314,14 +327,7 @@ __device__ __forceinline__ March hdda(const DevGrid &g, F3 src, F3 dir) {
         while ((st = ray_step<false>(g, r)) == 0xFFu) {
         }
     }
-    March m;
-    m.p = f3(r.px, r.py, r.pz);
-    m.state = st;
-    m.np = r.np;
-    m.node = ray_node(r);
-    m.i = r.i;
-    m.mask = ray_mask(r);
-    return m;
+    return march_result(r, st);
 }
 
 __device__ __forceinline__ F3 maskf(uint32_t m) {
@@ -396,6 +402,9 @@ __device__ __forceinline__ F3 grid_tint(const wx_state_uniform &s, F3 p) {
     return splat(0.0f);
 }
 
+// I_a of mode 3 (:186), the colour of a shadowed lit pixel.
+__device__ __forceinline__ F3 ambient_colour() { return (kKa * f3(0.4f, 0.4f, 0.3f)) * f3(0.4f, 0.2f, 0.2f); }
+
 // Colour of a finished primary ray for modes 0-2 and the non-lit part of
 // modes 0-3 (:156-194 for state 0, :231-262 for state 1, :264 otherwise).
 // For mode 3 with a hit, *need_shadow tells the caller to trace the shadow
@@ -420,7 +429,7 @@ __device__ __forceinline__ F3 primary_colour(const wx_state_uniform &s, const Ma
             const F3 N = normalize3((-step) * m);
             const float LN = pmax(0.0f, s.sun_color[3] * dot3(-sun, N));
             const F3 I_d = ((kKd * sc) * f3(0.4f, 0.2f, 0.2f)) * LN;
-            const F3 I_a = (kKa * f3(0.4f, 0.4f, 0.3f)) * f3(0.4f, 0.2f, 0.2f);
+            const F3 I_a = ambient_colour();
             if (LN != 0.0f) {
                 *need_shadow = true;
                 *shadowed_colour = I_a;
