@@ -385,6 +385,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the mixed-load batched comparison")
+    ap.add_argument("--no-surface", action="store_true", help="skip the zero-crossing mode (render mode 5) figure")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default launch shape instead of autotuning on 4 frames")
     ap.add_argument("--serve", action="store_true", help="run the serving sweep (config 5) instead")
@@ -531,6 +532,38 @@ def main():
         shadow = {"rays_per_step": n_sh, "value": world * n_sh / (ms / 1e3) / 1e9, "unit": "Grays/s",
                   "note": "shadow rays traced in the timed launches, rate over the same time; not part of value"}
 
+    # Zero-crossing hit mode (render mode 5, an extension with no reference counterpart): the same
+    # frames with level-set values attached; reported separately, not part of `value`.
+    surface = None
+    if args.workload in ("sphere", "spheres") and not args.no_surface:
+        t0 = time.perf_counter()
+        vals = W.spheres_values(topo) if args.workload == "spheres" else W.sphere_values(topo)
+        grid.set_values(vals, 3.0)
+        t_vals = time.perf_counter() - t0
+        del vals
+        st5 = []
+        for st in states:
+            c = wx.state_from_bytes(wx.state_bytes(st))
+            c.render_mode[0] = 5
+            st5.append(c)
+        for c, o in zip(st5, outs):
+            ctx.render(grid, c, W_, H_, o, None, stream=sh)
+        sm = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for c, o in zip(st5, outs):
+                ctx.render(grid, c, W_, H_, o, None, stream=sh)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            sm.append(e0.elapsed_time(e1))
+        s_ms = max_over_ranks(statistics.mean(sm), dist, dev)
+        surface = {"value": replica_throughput(rays_step, world, s_ms), "unit": "Grays/s", "ms_per_step": s_ms,
+                   "render_mode": 5, "values_bytes": int(info["n3"]) * 512 * 4, "values_host_s": round(t_vals, 2),
+                   "note": "zero-crossing hit mode (extension, no reference counterpart): primary HDDA, then "
+                           "trilinear level-set search and secant; not part of value"}
+
     # BASELINE config 4: batched vs plain on the mixed-resolution load (needs the 2000-sphere grid)
     batched = None
     if not args.no_batched and args.workload == "spheres":
@@ -578,7 +611,7 @@ def main():
                        "autotune": tuned and {"table [kernel, tile_w, warps/block, ms for 4 frames]": tuned["table"],
                                               "seconds": tuned["seconds"]}},
             "frame_latency_ms": {"p50": p50, "p99": p99},
-            "batched": batched, "shadow_rays": shadow,
+            "batched": batched, "shadow_rays": shadow, "surface": surface,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "gpu_launches": len(frames) * args.steps,
             "clocks": clk.summary(),

@@ -44,6 +44,15 @@ extern "C" {
 #define WX_MODE_RAY 2u
 #define WX_MODE_DIFFUSE 3u
 #define WX_MODE_GLOSSY 4u
+/* Extension, no reference counterpart: after the primary HDDA hit, search the
+ * zero crossing of the grid's level-set values (wx_grid_set_values) along the
+ * ray: samples every 0.25 voxel from 1 voxel before the hit, 64 at most,
+ * trilinear values, secant between the last positive and the first
+ * non-positive sample; Lambert colour of mode 3 with the trilinear gradient as
+ * normal and no shadow ray. wx_hit: p, t, node and info of the HDDA hit;
+ * shadow = found | sample index << 8; reserved = the crossing's t as float
+ * bits (NaN when none was found, and the colour is then mode 0's). */
+#define WX_MODE_SURFACE 5u
 
 /* 256-byte uniform; field order and padding of ComputeState
  * (src/render/gpu_types/compute_state.rs:9-29). Matrices are column-major. */
@@ -144,6 +153,12 @@ int wx_grid_build(wx_ctx *ctx, wx_topology *topo, wx_grid **out);
  * memory: about 4 bytes per leaf voxel plus 200 bytes per node. */
 int wx_grid_build_gpu(wx_ctx *ctx, const wx_topology *topo, wx_grid **out);
 int wx_grid_release(wx_ctx *ctx, wx_grid *grid);
+/* Attaches level-set values for WX_MODE_SURFACE: one float per leaf voxel
+ * (n3 * 512, DFS leaf order, voxel order x<<6 | y<<3 | z), the signed distance
+ * in voxel units, negative inside; voxels outside leaves read +band, or -band
+ * inside an active tile. Replaces earlier values; freed with the grid. No
+ * reference counterpart (the reference's raycast reads no values). */
+int wx_grid_set_values(wx_ctx *ctx, wx_grid *grid, const float *values, float band);
 int wx_grid_get_info(const wx_grid *grid, wx_grid_info *out);
 /* Copies a grid's device pools to host memory; any pointer may be NULL.
  * slot5: n5*32768 u32, slot4: n4*4096 u32 (bit 31 = child index, else the skip
@@ -210,7 +225,7 @@ int wx_batch_destroy(wx_batch *batch);
  * caller must serialise them. The call blocks until earlier work on `stream`
  * is done, because the frame table is copied from pageable host memory. */
 #define WX_NOALLOC_MAX_FRAMES 256
-#define WX_NOALLOC_SCRATCH_BYTES 90368 /* 256 + 256 frames x 352-byte table entries */
+#define WX_NOALLOC_SCRATCH_BYTES 94464 /* 256 + 256 frames x 368-byte table entries */
 int wx_render_batch_noalloc(const wx_frame *frames, uint32_t n, void *stream);
 
 /* ---- serving: continuous batching of render requests (no counterpart in the
@@ -338,6 +353,13 @@ int wx_gen_sphere(float cx, float cy, float cz, float radius, float band, wx_top
 /* Union of `count` spheres, radii U[rmin, rmax], centres U[lo, hi)^3. */
 int wx_gen_spheres(uint32_t count, float rmin, float rmax, float lo, float hi, float band,
                    uint64_t seed, wx_topology **out);
+/* Level-set values of those generators for every leaf voxel of `topo` (the
+ * layout of wx_grid_set_values): min over the spheres of |ijk - c| - r,
+ * clamped to [-band, band]. Same arguments as the generator that built topo. */
+int wx_gen_sphere_values(const wx_topology *topo, float cx, float cy, float cz, float radius, float band,
+                         float *values);
+int wx_gen_spheres_values(const wx_topology *topo, uint32_t count, float rmin, float rmax, float lo, float hi,
+                          float band, uint64_t seed, float *values);
 /* Leaves on the 8^3 lattice of [lo, lo + extent)^3 kept where 3-octave value
  * noise exceeds the quantile giving `occupancy`; voxels active with p_voxel. */
 int wx_gen_noise_leaves(int32_t lo, uint32_t extent, double occupancy, double p_voxel,

@@ -24,7 +24,8 @@ STATS_DTYPE = np.dtype([("steps", "<u4"), ("bytes", "<u4"), ("shadow_steps", "<u
 class orc_view(C.Structure):
     _fields_ = [("kids5", C.c_void_p), ("vals5", C.c_void_p), ("kids4", C.c_void_p), ("vals4", C.c_void_p),
                 ("vals3", C.c_void_p), ("origins", C.c_void_p), ("n5", C.c_uint64), ("n4", C.c_uint64),
-                ("n3", C.c_uint64), ("atlas", C.c_void_p * 3), ("dims", (C.c_uint32 * 3) * 3)]
+                ("n3", C.c_uint64), ("atlas", C.c_void_p * 3), ("dims", (C.c_uint32 * 3) * 3),
+                ("values", C.c_void_p), ("band", C.c_float)]
 
 
 _lib = None
@@ -186,7 +187,13 @@ def _view_struct(v: dict):
         s.atlas[i] = atl[i].ctypes.data
         for j in range(3):
             s.dims[i][j] = int(v["dims"][i][j])
-    return s, (keep, org, atl)
+    vals = None
+    if v.get("values") is not None:  # zero-crossing mode: n3 * 512 level-set values and their band
+        vals = np.ascontiguousarray(v["values"], np.float32)
+        assert vals.size == s.n3 * 512
+        s.values = vals.ctypes.data
+        s.band = float(v["band"])
+    return s, (keep, org, atl, vals)
 
 
 def render(v: dict, state: bytes, width: int, height: int, nthreads: int = 1, hits: bool = True,

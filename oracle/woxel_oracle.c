@@ -832,6 +832,8 @@ typedef struct {
     const orc_view *v;
     const orc_state *s;
     uint32_t shadow_traced, shadow_state, shadow_steps, shadow_bytes;
+    uint32_t surf_found, surf_k;  /* mode 5: crossing found, sample index */
+    float surf_t;
 } Ctx;
 
 static v3 sun3(const orc_state *s) { return V3(s->sun_dir[0], s->sun_dir[1], s->sun_dir[2]); }
@@ -895,6 +897,111 @@ static v3 reflect_ray2(Ctx *c, v3 src, v3 dir) { /* :267-309 */
     return dir;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Zero-crossing hit mode (render_mode 5). An extension with no counterpart in */
+/* the reference (its hit is the first active voxel); the product kernel      */
+/* follows this specification operation for operation:                        */
+/*   phi(i,j,k): the leaf value of voxel (i,j,k); -band inside an active tile  */
+/*     (value bit of an N5/N4 slot); +band anywhere else;                     */
+/*   phi(q) for a point q: trilinear in the cell floor(q) .. floor(q) + 1;     */
+/*   search: from t0 = max(0, t_hit - 1), where t_hit = dot(p_hit - eye, dir)  */
+/*     of the primary HDDA hit, samples t_k = t0 + k * 0.25 for k < 64; the    */
+/*     first k with phi(t_k) <= 0 ends it (k = 0: t* = t0; else the secant     */
+/*     t* = t_{k-1} + 0.25 * (phi_{k-1} / (phi_{k-1} - phi_k)));              */
+/*   normal: the gradient of the trilinear phi at eye + t* dir, normalised     */
+/*     (-dir when it is zero); colour: mode 3's I_a + I_d with that normal and */
+/*     no shadow ray; no crossing: mode 0's colour of the HDDA hit.            */
+/* ------------------------------------------------------------------------ */
+#define SURF_H 0.25f
+#define SURF_N 64u
+
+static float surf_phi(const orc_view *v, int32_t i, int32_t j, int32_t k) {
+    const float band = v->band;
+    const int32_t pos[3] = {i, j, k};
+    const int32_t g[3] = {g2n(i, 12), g2n(j, 12), g2n(k, 12)};
+    uint64_t n5 = UINT64_MAX;
+    for (uint64_t a = 0; a < v->n5; a++) {
+        const int32_t *o = v->origins + 4 * a;
+        if (o[0] == g[0] && o[1] == g[1] && o[2] == g[2]) { n5 = a; break; }
+    }
+    if (n5 == UINT64_MAX) return band;
+    uint32_t c5[3] = {((uint32_t)pos[0] & 4095u) >> 7, ((uint32_t)pos[1] & 4095u) >> 7, ((uint32_t)pos[2] & 4095u) >> 7};
+    uint32_t off5 = (c5[0] << 10) | (c5[1] << 5) | c5[2];
+    if (bit(v->vals5 + 1024ull * n5, off5)) return -band;
+    if (!bit(v->kids5 + 1024ull * n5, off5)) return band;
+    uint32_t d5 = v->dims[0][1] >> 5;
+    uint32_t n4 = tex_load(v, 0, c5[0] + 32 * (uint32_t)(n5 % d5), c5[1] + 32 * (uint32_t)((n5 / d5) % d5),
+                           c5[2] + 32 * (uint32_t)(n5 / (d5 * d5)));
+    uint32_t c4[3] = {((uint32_t)pos[0] & 127u) >> 3, ((uint32_t)pos[1] & 127u) >> 3, ((uint32_t)pos[2] & 127u) >> 3};
+    uint32_t off4 = (c4[0] << 8) | (c4[1] << 4) | c4[2];
+    if (bit(v->vals4 + 128ull * n4, off4)) return -band;
+    if (!bit(v->kids4 + 128ull * n4, off4)) return band;
+    uint32_t d4 = v->dims[1][0] >> 4;
+    uint32_t n3 = tex_load(v, 1, c4[0] + 16 * (n4 % d4), c4[1] + 16 * ((n4 / d4) % d4), c4[2] + 16 * (n4 / (d4 * d4)));
+    uint32_t off3 = (((uint32_t)pos[0] & 7u) << 6) | (((uint32_t)pos[1] & 7u) << 3) | ((uint32_t)pos[2] & 7u);
+    return v->values[512ull * n3 + off3];
+}
+
+static inline float lerpf(float a, float b, float t) { return a + t * (b - a); }
+
+/* The 8 corner values of the cell of q and q's position inside it. */
+static void surf_cell(const orc_view *v, v3 q, float c[8], float f[3]) {
+    float fl[3] = {floorf(q.x), floorf(q.y), floorf(q.z)};
+    int32_t i = f2i_sat(fl[0]), j = f2i_sat(fl[1]), k = f2i_sat(fl[2]);
+    f[0] = q.x - fl[0]; f[1] = q.y - fl[1]; f[2] = q.z - fl[2];
+    for (int n = 0; n < 8; n++)  /* corner n = (dx << 2) | (dy << 1) | dz */
+        c[n] = surf_phi(v, i + (n >> 2), j + ((n >> 1) & 1), k + (n & 1));
+}
+
+static float surf_interp(const float c[8], const float f[3]) {
+    float a00 = lerpf(c[0], c[4], f[0]), a10 = lerpf(c[2], c[6], f[0]);
+    float a01 = lerpf(c[1], c[5], f[0]), a11 = lerpf(c[3], c[7], f[0]);
+    return lerpf(lerpf(a00, a10, f[1]), lerpf(a01, a11, f[1]), f[2]);
+}
+
+static v3 surf_gradient(const float c[8], const float f[3]) {
+    float gx = lerpf(lerpf(c[4] - c[0], c[6] - c[2], f[1]), lerpf(c[5] - c[1], c[7] - c[3], f[1]), f[2]);
+    float gy = lerpf(lerpf(c[2] - c[0], c[6] - c[4], f[0]), lerpf(c[3] - c[1], c[7] - c[5], f[0]), f[2]);
+    float gz = lerpf(lerpf(c[1] - c[0], c[5] - c[4], f[0]), lerpf(c[3] - c[2], c[7] - c[6], f[0]), f[1]);
+    return V3(gx, gy, gz);
+}
+
+static float surf_sample(const orc_view *v, v3 eye, v3 dir, float t) {
+    float c[8], f[3];
+    surf_cell(v, V3(eye.x + t * dir.x, eye.y + t * dir.y, eye.z + t * dir.z), c, f);
+    return surf_interp(c, f);
+}
+
+/* Returns 1 and t*, the sample index and the normal when a crossing is found. */
+static int surf_search(const orc_view *v, v3 eye, v3 dir, float t_hit, float *ts, uint32_t *ks, v3 *N) {
+    if (!v->values) return 0;
+    float t0 = t_hit - 1.0f;
+    if (!(t0 > 0.0f)) t0 = 0.0f;
+    float prev = surf_sample(v, eye, dir, t0);
+    int found = 0;
+    if (prev <= 0.0f) {
+        *ts = t0; *ks = 0; found = 1;
+    } else {
+        for (uint32_t k = 1; k < SURF_N; k++) {
+            float tk = t0 + (float)k * SURF_H;
+            float ph = surf_sample(v, eye, dir, tk);
+            if (ph <= 0.0f) {
+                float tp = t0 + (float)(k - 1) * SURF_H;
+                *ts = tp + SURF_H * (prev / (prev - ph));
+                *ks = k; found = 1;
+                break;
+            }
+            prev = ph;
+        }
+    }
+    if (!found) return 0;
+    float c[8], f[3];
+    surf_cell(v, V3(eye.x + *ts * dir.x, eye.y + *ts * dir.y, eye.z + *ts * dir.z), c, f);
+    v3 g = surf_gradient(c, f);
+    *N = vdot(g, g) == 0.0f ? vneg(dir) : vnormalize(g);
+    return 1;
+}
+
 static v3 ray_trace(Ctx *c, v3 src, v3 dir, HDDAout *primary) { /* :152-265 */
     const orc_state *s = c->s;
     HDDAout hit = hdda_ray(c->v, src, dir);
@@ -949,6 +1056,21 @@ static v3 ray_trace(Ctx *c, v3 src, v3 dir, HDDAout *primary) { /* :152-265 */
                 v3 rsrc = vsub(hit.p, vmul(vscale(4e-2f, step), m));
                 v3 rcol = reflect_ray2(c, rsrc, rdir);
                 return vmix(mcol, rcol, REFLECTIVITY);
+            }
+            case 5u: {
+                float ts;
+                uint32_t ks;
+                v3 N;
+                v3 d = vsub(hit.p, src);
+                if (surf_search(c->v, src, dir, vdot(d, dir), &ts, &ks, &N)) {
+                    c->surf_found = 1; c->surf_k = ks; c->surf_t = ts;
+                    float LN = pmax(0.0f, s->sun_color[3] * vdot(vneg(sun3(s)), N));
+                    v3 I_d = vscale_r(vmul(vscale(K_D, suncol3(s)), V3(0.4f, 0.2f, 0.2f)), LN);
+                    v3 I_a = vmul(vscale(K_A, V3(0.4f, 0.4f, 0.3f)), V3(0.4f, 0.2f, 0.2f));
+                    return vadd(I_a, I_d);
+                }
+                v3 a = vmul(m, V3(0.2f, 0.2f, 0.3f));
+                return vsplat((a.x + a.y) + a.z);
             }
             default: {
                 v3 a = vmul(m, V3(0.2f, 0.2f, 0.3f));
@@ -1015,6 +1137,13 @@ static void shade_pixel(const orc_view *v, const orc_state *s, uint32_t gx, uint
                   ((uint32_t)prim.mask[1] << 5) | ((uint32_t)prim.mask[2] << 6) | (prim.i << 8);
         h->shadow = c.shadow_traced ? (1u | (c.shadow_state << 1) | (c.shadow_steps << 8)) : 0u;
         h->reserved = 0;
+        if (s->render_mode[0] == 5u) {  /* zero-crossing: found | sample index << 8, t* bits */
+            h->shadow = c.surf_found ? (1u | (c.surf_k << 8)) : 0u;
+            uint32_t tb;
+            float tsv = c.surf_found ? c.surf_t : NAN;
+            memcpy(&tb, &tsv, 4);
+            h->reserved = c.surf_found ? tb : 0x7FC00000u;
+        }
     }
     if (stats) {
         orc_stats *st = &stats[pix];

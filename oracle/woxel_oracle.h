@@ -83,6 +83,12 @@ typedef struct orc_view {
     uint64_t n5, n4, n3;
     const uint32_t *atlas[3];        /* N5, N4, N3 atlases, texel (x,y,z) at (z*H + y)*W + x */
     uint32_t dims[3][3];             /* W, H, D of each atlas */
+    /* Zero-crossing mode (render_mode 5, no reference counterpart): level-set value of
+       every leaf voxel (n3 * 512, DFS leaf order, voxel x<<6 | y<<3 | z) and the band
+       that voxels outside leaves read (+band, or -band inside an active tile). NULL:
+       mode 5 finds no crossing. */
+    const float *values;
+    float band;
 } orc_view;
 
 typedef struct orc_tree orc_tree;

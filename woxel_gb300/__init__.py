@@ -22,7 +22,7 @@ HIT_DTYPE = np.dtype([("p", "<f4", (3,)), ("t", "<f4"), ("node", "<u4"), ("info"
                       ("shadow", "<u4"), ("reserved", "<u4")])
 assert HIT_DTYPE.itemsize == 32
 
-MODE_GRAY, MODE_RGB, MODE_RAY, MODE_DIFFUSE, MODE_GLOSSY = 0, 1, 2, 3, 4
+MODE_GRAY, MODE_RGB, MODE_RAY, MODE_DIFFUSE, MODE_GLOSSY, MODE_SURFACE = 0, 1, 2, 3, 4, 5
 
 
 def _ptr(a) -> Optional[int]:
@@ -110,6 +110,18 @@ class Topology:
         return cls._make(lib().wx_topology_from_masks, arrs["kids5"].ctypes.data, arrs["vals5"].ctypes.data, n5,
                          arrs["kids4"].ctypes.data, arrs["vals4"].ctypes.data, n4, arrs["vals3"].ctypes.data, n3,
                          org.ctypes.data, stride)
+
+    def sphere_values(self, center=(0.0, 0.0, 0.0), radius=64.0, band=3.0) -> np.ndarray:
+        """Level-set values (n3 * 512 float32, wx_grid_set_values layout) of Topology.sphere's grid."""
+        out = np.empty(self.counts[2] * 512, np.float32)
+        check(lib().wx_gen_sphere_values(self._h, *map(float, center), float(radius), float(band), out.ctypes.data))
+        return out
+
+    def spheres_values(self, count=2000, rmin=4.0, rmax=40.0, lo=-1024.0, hi=1024.0, band=3.0, seed=2) -> np.ndarray:
+        """Level-set values of Topology.spheres' grid (same arguments)."""
+        out = np.empty(self.counts[2] * 512, np.float32)
+        check(lib().wx_gen_spheres_values(self._h, count, rmin, rmax, lo, hi, band, seed, out.ctypes.data))
+        return out
 
     def close(self) -> None:
         if self._h and self._h.value:
@@ -213,6 +225,13 @@ class Grid:
         i = wx_grid_info()
         check(lib().wx_grid_get_info(self._h, C.byref(i)))
         return {k: int(getattr(i, k)) for k, _ in wx_grid_info._fields_}
+
+    def set_values(self, values: np.ndarray, band: float) -> None:
+        """Level-set values for MODE_SURFACE (n3 * 512 float32, DFS leaf order)."""
+        v = np.ascontiguousarray(values, np.float32)
+        if v.size != self.info["n3"] * 512:
+            raise ValueError("need n3 * 512 values")
+        check(lib().wx_grid_set_values(self.ctx._h, self._h, v.ctypes.data, float(band)), self.ctx._h)
 
     def pools(self) -> dict:
         """Copies of the device pools: slot5, slot4 (u32), leaf (u8) and ovf ((key, distance) u32 pairs)."""
@@ -351,7 +370,7 @@ def render_batch_noalloc(frames: Sequence, stream=None) -> None:
     """wx_render_batch_noalloc: a batch rendered without any allocation or context.
 
     For callers that cannot allocate device memory while rendering; scratch is a
-    fixed 90,368-byte device array inside the library (at most 256 frames a call).
+    fixed 94,464-byte device array inside the library (at most 256 frames a call).
     The first call on a device sets that device up; overlapping calls race.
     """
     arr = Context._frames(frames)

@@ -92,6 +92,7 @@ SIGNATURES = {
     "wx_grid_build_gpu": (INT, [P, P, C.POINTER(P)]),
     "wx_grid_read_pools": (INT, [P, P, P, P, P, P, C.POINTER(C.c_uint64)]),
     "wx_grid_release": (INT, [P, P]),
+    "wx_grid_set_values": (INT, [P, P, P, F32]),
     "wx_grid_get_info": (INT, [P, C.POINTER(wx_grid_info)]),
     "wx_render": (INT, [P, P, C.POINTER(wx_state_uniform), U32, U32, P, P, P]),
     "wx_ctx_set_tuning": (INT, [P, C.POINTER(wx_tuning)]),
@@ -129,6 +130,8 @@ SIGNATURES = {
     "wx_topology_atlas": (INT, [P, P, P, P, P, U32]),
     "wx_gen_sphere": (INT, [F32, F32, F32, F32, F32, C.POINTER(P)]),
     "wx_gen_spheres": (INT, [U32, F32, F32, F32, F32, F32, U64, C.POINTER(P)]),
+    "wx_gen_sphere_values": (INT, [P, F32, F32, F32, F32, F32, P]),
+    "wx_gen_spheres_values": (INT, [P, U32, F32, F32, F32, F32, F32, U64, P]),
     "wx_gen_noise_leaves": (INT, [I32, U32, C.c_double, C.c_double, U64, INT, C.POINTER(P)]),
     "wx_orbit_eyes": (INT, [U32, F32, U64, P]),
     "wx_vdb_read_topology": (INT, [C.c_char_p, C.c_char_p, C.POINTER(P), C.POINTER(wx_vdb_info)]),

@@ -61,6 +61,7 @@ struct wx_grid {
     int device = 0;
     void *dev = nullptr;
     size_t bytes = 0;
+    float *values = nullptr;  // level-set values (zero-crossing mode), own allocation
     wxk::DevGrid g{};
     wx_grid_info info{};
 };
@@ -230,6 +231,7 @@ int alloc_grid(wx_ctx *ctx, const std::vector<int4> &o5, uint64_t n5, uint64_t n
 void free_grid(wx_grid *gr) {
     if (!gr) return;
     cudaFree(gr->dev);
+    if (gr->values) cudaFree(gr->values);
     delete gr;
 }
 
@@ -772,8 +774,25 @@ int wx_grid_release(wx_ctx *ctx, wx_grid *grid) {
     if (!grid) return WX_OK;
     cudaSetDevice(grid->device);
     cudaError_t e = cudaFree(grid->dev);
+    if (grid->values) {
+        const cudaError_t e2 = cudaFree(grid->values);
+        if (e == cudaSuccess) e = e2;
+    }
     delete grid;
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaFree(node pools)");
+    return WX_OK;
+}
+
+int wx_grid_set_values(wx_ctx *ctx, wx_grid *grid, const float *values, float band) {
+    if (!ctx || !grid || !values) return fail(ctx, WX_ERR_INVALID, "wx_grid_set_values: null argument");
+    if (!(band > 0.0f) || !(band < 3.0e38f))
+        return fail(ctx, WX_ERR_INVALID, "wx_grid_set_values: band must be positive and finite");
+    WX_CUDA(ctx, cudaSetDevice(grid->device));
+    const size_t bytes = (size_t)grid->info.n3 * wx::kN3Slots * sizeof(float);
+    if (!grid->values && bytes) WX_CUDA(ctx, cudaMalloc(&grid->values, bytes));
+    if (bytes) WX_CUDA(ctx, cudaMemcpy(grid->values, values, bytes, cudaMemcpyHostToDevice));
+    grid->g.values = grid->values;
+    grid->g.band = band;
     return WX_OK;
 }
 
@@ -888,7 +907,7 @@ int wx_render_batch(wx_ctx *ctx, const wx_frame *frames, uint32_t n, void *strea
                                  cudaMemcpyHostToDevice, st));
     WX_CUDA(ctx, cudaEventRecord(ctx->jobs_done, st));
     WX_CUDA(ctx, wxk::launch_batched(ctx->jobs_dev, (uint32_t)jobs.size(), total, ctx->take_counter(), ctx->tuning,
-                                     ctx->num_sms, st));
+                                     ctx->num_sms, wxk::all_modes(jobs.data(), jobs.size()), st));
     return WX_OK;
 }
 
@@ -925,7 +944,7 @@ int wx_batch_create(wx_ctx *ctx, const wx_frame *frames, uint32_t n, wx_batch **
         return bail(e, "cudaStreamBeginCapture");
     }
     cudaError_t le = b->njobs ? wxk::launch_batched(b->jobs_dev, b->njobs, total, b->counter, ctx->tuning,
-                                                    ctx->num_sms, cs)
+                                                    ctx->num_sms, wxk::all_modes(jobs.data(), jobs.size()), cs)
                               : cudaMemsetAsync(b->counter, 0, sizeof(uint32_t), cs);
     e = cudaStreamEndCapture(cs, &b->graph);
     cudaStreamDestroy(cs);

@@ -26,7 +26,10 @@ using wxk::Job;
 // cp_main for one pixel of job J: colour, optional hit record, shadow ray (mode 3)
 // or the glossy chain (mode 4). Tile tl of the job covers tile_w x tile_h
 // pixels; lanes outside the dispatched region 8*floor(w/8) x 4*floor(h/4)
-// (wgpu_context.rs:281) do nothing.
+// (wgpu_context.rs:281) do nothing. kAll = false compiles modes 0-3 only (the
+// host sends frames of modes 4 and 5 to the kAll = true kernels): the glossy
+// chain and the zero-crossing search would otherwise cost the march registers.
+template <bool kAll>
 __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t lane) {
     const uint32_t gx = (tl % J.tiles_x) * J.tile_w + lane % J.tile_w;
     const uint32_t gy = (tl / J.tiles_x) * J.tile_h + lane / J.tile_w;
@@ -42,10 +45,29 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
     const March hit = hdda(J.g, eye, dir);
     __syncwarp(act);
     F3 c;
-    uint32_t shadow = 0;
-    if (s.render_mode[0] == 4u) {
+    uint32_t shadow = 0, reserved = 0;
+    if (kAll && s.render_mode[0] == 4u) {
         c = glossy_colour(J.g, s, hit, dir);
-    } else {
+    } else if (kAll && s.render_mode[0] == 5u) {  // zero crossing (extension); the mode is warp-uniform
+        reserved = 0x7FC00000u;           // NaN: no crossing
+        if (hit.state == 0u) {
+            float ts;
+            uint32_t ks;
+            F3 N;
+            if (surf_search(J.g, eye, dir, dot3(hit.p - eye, dir), &ts, &ks, &N)) {
+                c = surface_colour(s, N);
+                shadow = 1u | (ks << 8);
+                reserved = __float_as_uint(ts);
+            } else {
+                const F3 a = maskf(hit.mask) * f3(0.2f, 0.2f, 0.3f);
+                c = splat((a.x + a.y) + a.z);
+            }
+        } else {
+            bool need;
+            F3 shadowed, src;
+            c = primary_colour(s, hit, dir, &need, &shadowed, &src);  // states 1, 2: mode 3's colours
+        }
+    } else {  // modes 0-3: every valid lane of the warp comes here (the __syncwarp below needs them all)
         bool need;
         F3 shadowed, src;
         c = primary_colour(s, hit, dir, &need, &shadowed, &src);
@@ -61,7 +83,7 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
     J.rgba[pix] = pack_rgba(c);
     if (J.hits)
         store_hit(J.hits + pix, hit.p, dot3(hit.p - eye, dir), hit.node,
-                  hit.state | (hit.np << 2) | (hit.mask << 4) | (hit.i << 8), shadow);
+                  hit.state | (hit.np << 2) | (hit.mask << 4) | (hit.i << 8), shadow, reserved);
 }
 
 // One warp per tile, tiles in launch order.
@@ -71,10 +93,11 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
 // spills outside the march loop; 40 registers spill too much.
 #define WX_RAY_BOUNDS __launch_bounds__(256, 5)
 
+template <bool kAll>
 __global__ void WX_RAY_BOUNDS k_pixel(const __grid_constant__ Job job, uint32_t ntiles) {
     const uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (tile >= ntiles) return;
-    render_pixel(job, tile, threadIdx.x & 31u);
+    render_pixel<kAll>(job, tile, threadIdx.x & 31u);
 }
 
 // First job whose tile range contains tile t (jobs sorted by tile_begin, no empty jobs).
@@ -92,7 +115,7 @@ __device__ __forceinline__ uint32_t find_job(const Job *__restrict__ jobs, uint3
 // Persistent warps drawing whole tiles from a global queue (one atomic per
 // 32 rays). Tiles are numbered job by job; a warp's successive tiles increase,
 // so its job search starts at the previous job.
-template <bool kBatched>
+template <bool kBatched, bool kAll>
 __global__ void WX_RAY_BOUNDS k_persistent(const Job *__restrict__ jobs, uint32_t njobs, const __grid_constant__ Job job0,
                              uint32_t total_tiles, uint32_t *__restrict__ ctr) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -105,9 +128,9 @@ __global__ void WX_RAY_BOUNDS k_persistent(const Job *__restrict__ jobs, uint32_
         if (kBatched) {
             cur_job = find_job(jobs, njobs, t, cur_job);
             const Job &J = jobs[cur_job];
-            render_pixel(J, t - J.tile_begin + J.tile_off, lane);
+            render_pixel<kAll>(J, t - J.tile_begin + J.tile_off, lane);
         } else {
-            render_pixel(job0, t, lane);
+            render_pixel<kAll>(job0, t, lane);
         }
     }
 }
@@ -157,13 +180,15 @@ cudaError_t init_device_tables() {
 
 int max_blocks_per_sm(int kernel, bool batched, int warps_per_block) {
     const int threads = 32 * warps_per_block;
-    if (kernel == 1) return blocks_for(k_pixel, threads);
-    return batched ? blocks_for(k_persistent<true>, threads) : blocks_for(k_persistent<false>, threads);
+    if (kernel == 1) return blocks_for(k_pixel<false>, threads);
+    return batched ? blocks_for(k_persistent<true, false>, threads) : blocks_for(k_persistent<false, false>, threads);
 }
 
 cudaError_t launch_pixel(const Job &job, const Tuning &t, cudaStream_t st) {
     const uint32_t wpb = (uint32_t)t.warps_per_block;
-    k_pixel<<<(job.tiles + wpb - 1) / wpb, 32 * wpb, 0, st>>>(job, job.tiles);
+    const unsigned blocks = (job.tiles + wpb - 1) / wpb;
+    if (all_modes(job.s)) k_pixel<true><<<blocks, 32 * wpb, 0, st>>>(job, job.tiles);
+    else k_pixel<false><<<blocks, 32 * wpb, 0, st>>>(job, job.tiles);
     return cudaGetLastError();
 }
 
@@ -178,19 +203,33 @@ static int grid_blocks(const Tuning &t, bool batched, int num_sms, uint32_t tota
 cudaError_t launch_persistent(const Job &job, uint32_t *ctr, const Tuning &t, int num_sms, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    k_persistent<false><<<grid_blocks(t, false, num_sms, job.tiles), 32 * t.warps_per_block, 0, st>>>(
-        nullptr, 1, job, job.tiles, ctr);
+    const int blocks = grid_blocks(t, false, num_sms, job.tiles);
+    if (all_modes(job.s))
+        k_persistent<false, true><<<blocks, 32 * t.warps_per_block, 0, st>>>(nullptr, 1, job, job.tiles, ctr);
+    else
+        k_persistent<false, false><<<blocks, 32 * t.warps_per_block, 0, st>>>(nullptr, 1, job, job.tiles, ctr);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batched(const Job *jobs_dev, uint32_t njobs, uint32_t total_tiles, uint32_t *ctr,
-                           const Tuning &t, int num_sms, cudaStream_t st) {
+                           const Tuning &t, int num_sms, bool all, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     Job dummy{};
-    k_persistent<true><<<grid_blocks(t, true, num_sms, total_tiles), 32 * t.warps_per_block, 0, st>>>(
-        jobs_dev, njobs, dummy, total_tiles, ctr);
+    const int blocks = grid_blocks(t, true, num_sms, total_tiles);
+    if (all)
+        k_persistent<true, true><<<blocks, 32 * t.warps_per_block, 0, st>>>(jobs_dev, njobs, dummy, total_tiles, ctr);
+    else
+        k_persistent<true, false><<<blocks, 32 * t.warps_per_block, 0, st>>>(jobs_dev, njobs, dummy, total_tiles, ctr);
     return cudaGetLastError();
+}
+
+bool all_modes(const wx_state_uniform &s) { return s.render_mode[0] == 4u || s.render_mode[0] == 5u; }
+
+bool all_modes(const Job *jobs, size_t n) {
+    for (size_t i = 0; i < n; i++)
+        if (all_modes(jobs[i].s)) return true;
+    return false;
 }
 
 cudaError_t check_division(uint32_t max_m, unsigned long long *out_dev, cudaStream_t st) {
@@ -212,7 +251,7 @@ cudaError_t check_division(uint32_t max_m, unsigned long long *out_dev, cudaStre
 // deadline). wx_render_batch needs a context whose scratch (queue counters,
 // frame table) comes from cudaMalloc. This entry point instead keeps its
 // scratch in the fixed device array below, which the library declares
-// statically: every GPU that loads the library holds these 90,368 bytes until
+// statically: every GPU that loads the library holds these 94,464 bytes until
 // the process exits. Layout: the tile-queue counter at byte 0, the frame
 // (job) table from byte 256, room for WX_NOALLOC_MAX_FRAMES frames.
 // ---------------------------------------------------------------------------
@@ -312,7 +351,8 @@ int noalloc_render(int device, const wx_frame *frames, uint32_t n, cudaStream_t 
     cudaError_t e = cudaMemcpyAsync(jobs_dev, g_noalloc_table, njobs * sizeof(Job), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: frame table copy failed");
     wxk::Tuning t;  // defaults; launch_batched clears the counter (it keeps the last call's value otherwise)
-    e = wxk::launch_batched(jobs_dev, njobs, (uint32_t)tiles, counter, t, d->num_sms, st);
+    e = wxk::launch_batched(jobs_dev, njobs, (uint32_t)tiles, counter, t, d->num_sms,
+                            wxk::all_modes(g_noalloc_table, njobs), st);
     if (e != cudaSuccess) return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: launch failed");
     return WX_OK;
 }

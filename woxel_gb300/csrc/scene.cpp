@@ -85,15 +85,16 @@ static bool sphere_leaf(const I3 &o, const Sphere *s, const uint32_t *ids, size_
     return any;
 }
 
-static int spheres_to_topology(const std::vector<Sphere> &sph, double band, int nthreads,
-                               wx_topology **out) {
-    // Bin spheres into the leaves their band can touch.
-    struct H {
-        size_t operator()(const I3 &k) const {
-            return (size_t)mix64(((uint64_t)(uint32_t)k[0] << 32) | (uint32_t)k[1], (uint32_t)k[2]);
-        }
-    };
-    std::unordered_map<I3, std::vector<uint32_t>, H> bins;
+struct LeafHash {
+    size_t operator()(const I3 &k) const {
+        return (size_t)mix64(((uint64_t)(uint32_t)k[0] << 32) | (uint32_t)k[1], (uint32_t)k[2]);
+    }
+};
+using SphereBins = std::unordered_map<I3, std::vector<uint32_t>, LeafHash>;
+
+// The spheres whose band can touch each leaf, by leaf origin.
+static SphereBins bin_spheres(const std::vector<Sphere> &sph, double band) {
+    SphereBins bins;
     for (uint32_t i = 0; i < sph.size(); i++) {
         int32_t lo[3], hi[3];
         for (int a = 0; a < 3; a++) {
@@ -104,6 +105,12 @@ static int spheres_to_topology(const std::vector<Sphere> &sph, double band, int 
             for (int32_t y = lo[1]; y <= hi[1]; y += 8)
                 for (int32_t z = lo[2]; z <= hi[2]; z += 8) bins[I3{x, y, z}].push_back(i);
     }
+    return bins;
+}
+
+static int spheres_to_topology(const std::vector<Sphere> &sph, double band, int nthreads,
+                               wx_topology **out) {
+    const SphereBins bins = bin_spheres(sph, band);
     std::vector<I3> keys;
     keys.reserve(bins.size());
     for (auto &kv : bins) keys.push_back(kv.first);
@@ -284,19 +291,73 @@ int wx_gen_sphere(float cx, float cy, float cz, float radius, float band, wx_top
     return spheres_to_topology(s, band, 0, out);
 }
 
-int wx_gen_spheres(uint32_t count, float rmin, float rmax, float lo, float hi, float band,
-                   uint64_t seed, wx_topology **out) {
-    if (!out || !(rmin >= 0.0f) || !(rmax >= rmin) || !(hi > lo) || !(band > 0.0f)) {
-        set_thread_error("wx_gen_spheres: bad parameters");
-        return WX_ERR_INVALID;
-    }
+static std::vector<Sphere> sphere_list(uint32_t count, float rmin, float rmax, float lo, float hi, uint64_t seed) {
     Rng rng(seed);
     std::vector<Sphere> s(count);
     for (auto &q : s) {  // draw order per sphere: cx, cy, cz, r
         for (int a = 0; a < 3; a++) q.c[a] = lo + (hi - lo) * rng.uniform();
         q.r = rmin + (rmax - rmin) * rng.uniform();
     }
-    return spheres_to_topology(s, band, 0, out);
+    return s;
+}
+
+int wx_gen_spheres(uint32_t count, float rmin, float rmax, float lo, float hi, float band,
+                   uint64_t seed, wx_topology **out) {
+    if (!out || !(rmin >= 0.0f) || !(rmax >= rmin) || !(hi > lo) || !(band > 0.0f)) {
+        set_thread_error("wx_gen_spheres: bad parameters");
+        return WX_ERR_INVALID;
+    }
+    return spheres_to_topology(sphere_list(count, rmin, rmax, lo, hi, seed), band, 0, out);
+}
+
+// Level-set values of the sphere generators for every voxel of every leaf of
+// t, in DFS leaf order and voxel order x << 6 | y << 3 | z: the signed distance
+// min_s(|v - c_s| - r_s) (the quantity whose |.| < band made the voxel active),
+// clamped to [-band, band] as a narrow-band level set stores it.
+static int spheres_values(const wx_topology *t, const std::vector<Sphere> &sph, double band, float *out) {
+    SphereBins bins;
+    try {
+        bins = bin_spheres(sph, band);
+    } catch (...) {
+        set_thread_error("sphere values: host allocation failed");
+        return WX_ERR_OOM;
+    }
+    parallel_for(t->o3.size(), hw_threads(0), [&](size_t i) {
+        const I3 &o = t->o3[i];
+        const auto it = bins.find(o);
+        for (uint32_t v = 0; v < 512; v++) {
+            double d = INFINITY;
+            if (it != bins.end()) {
+                const double x = o[0] + (int)(v >> 6), y = o[1] + (int)((v >> 3) & 7), z = o[2] + (int)(v & 7);
+                for (uint32_t id : it->second) {
+                    const Sphere &q = sph[id];
+                    const double dx = x - q.c[0], dy = y - q.c[1], dz = z - q.c[2];
+                    d = std::min(d, std::sqrt(dx * dx + dy * dy + dz * dz) - q.r);
+                }
+            }
+            out[i * 512 + v] = (float)std::min(band, std::max(-band, d));
+        }
+    });
+    return WX_OK;
+}
+
+int wx_gen_sphere_values(const wx_topology *t, float cx, float cy, float cz, float radius, float band,
+                         float *values) {
+    if (!t || !values || !(radius >= 0.0f) || !(band > 0.0f)) {
+        set_thread_error("wx_gen_sphere_values: bad arguments");
+        return WX_ERR_INVALID;
+    }
+    std::vector<Sphere> s{{{cx, cy, cz}, radius}};
+    return spheres_values(t, s, band, values);
+}
+
+int wx_gen_spheres_values(const wx_topology *t, uint32_t count, float rmin, float rmax, float lo, float hi,
+                          float band, uint64_t seed, float *values) {
+    if (!t || !values || !(rmin >= 0.0f) || !(rmax >= rmin) || !(hi > lo) || !(band > 0.0f)) {
+        set_thread_error("wx_gen_spheres_values: bad arguments");
+        return WX_ERR_INVALID;
+    }
+    return spheres_values(t, sphere_list(count, rmin, rmax, lo, hi, seed), band, values);
 }
 
 int wx_gen_noise_leaves(int32_t lo, uint32_t extent, double occupancy, double p_voxel,

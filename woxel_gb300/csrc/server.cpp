@@ -232,7 +232,9 @@ struct wx_server {
         if (n == 0) return false;
         wxk::Tuning t;
         cudaError_t e = cudaMemcpyAsync(s.jobs_dev, s.jobs_host, n * sizeof(wxk::Job), cudaMemcpyHostToDevice, s.stream);
-        if (e == cudaSuccess) e = wxk::launch_batched(s.jobs_dev, n, tiles, s.counter, t, num_sms, s.stream);
+        if (e == cudaSuccess)
+            e = wxk::launch_batched(s.jobs_dev, n, tiles, s.counter, t, num_sms, wxk::all_modes(s.jobs_host, n),
+                                    s.stream);
         if (e == cudaSuccess) e = cudaEventRecord(s.ev, s.stream);
         if (e != cudaSuccess) {
             cudaGetLastError();

@@ -150,6 +150,31 @@ __device__ __noinline__ uint32_t leaf_overflow(const DevGrid &g, uint32_t key) {
     return lo < g.n_ovf ? __ldg(&g.ovf[lo].y) : 255u;
 }
 
+constexpr uint32_t kNoNode = 0xFFFFFFFFu;
+
+// Index of the N5 whose origin is (x, y, z) & ~4095, or kNoNode: the dense
+// table of root keys (the first matching origin of the shader's scan), or the
+// scan itself when the key box was too large for a table.
+__device__ __forceinline__ uint32_t root_find(const DevGrid &g, int x, int y, int z) {
+    const int4 h0 = __ldg(g.root), h1 = __ldg(g.root + 1);
+    if (h1.w) {
+        const uint32_t ux = (uint32_t)((x >> 12) - h0.x), uy = (uint32_t)((y >> 12) - h0.y),
+                       uz = (uint32_t)((z >> 12) - h0.z);
+        if (ux < (uint32_t)h0.w && uy < (uint32_t)h1.x && uz < (uint32_t)h1.y) {
+            const uint32_t *tab = reinterpret_cast<const uint32_t *>(g.root + 2 + g.n5);
+            const uint32_t e = __ldg(tab + (uz * (uint32_t)h1.x + uy) * (uint32_t)h0.w + ux);
+            if (e) return e - 1u;
+        }
+        return kNoNode;
+    }
+    const int kx = x & ~4095, ky = y & ~4095, kz = z & ~4095;
+    for (uint32_t k = 0; k < g.n5; k++) {
+        const int4 o = __ldg(g.root + 2 + k);
+        if (o.x == kx && o.y == ky && o.z == kz) return k;
+    }
+    return kNoNode;
+}
+
 // One loop iteration of hdda_ray. Returns 0xFF while the march continues,
 // otherwise the final state (0 hit, 1 out of bounds, 2 step cap); on return
 // r.i is the iteration count the shader reports. kCareful selects the
@@ -170,28 +195,10 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     uint32_t dist = 1;
     if (lvl == 0) {  // get_vdb_leaf_from_nothing (:398-413): the N5 whose origin is floor(p) & ~4095
         r.np = 0;
-        const int4 h0 = __ldg(g.root), h1 = __ldg(g.root + 1);
-        if (h1.w) {  // dense table of root keys (the first matching origin of the scan)
-            const uint32_t ux = (uint32_t)((x >> 12) - h0.x), uy = (uint32_t)((y >> 12) - h0.y),
-                           uz = (uint32_t)((z >> 12) - h0.z);
-            if (ux < (uint32_t)h0.w && uy < (uint32_t)h1.x && uz < (uint32_t)h1.y) {
-                const uint32_t *tab = reinterpret_cast<const uint32_t *>(g.root + 2 + g.n5);
-                const uint32_t e = __ldg(tab + (uz * (uint32_t)h1.x + uy) * (uint32_t)h0.w + ux);
-                if (e) {
-                    r.i5 = e - 1u;
-                    lvl = 5;
-                }
-            }
-        } else {  // linear scan, as the shader
-            const int kx = x & ~4095, ky = y & ~4095, kz = z & ~4095;
-            for (uint32_t k = 0; k < g.n5; k++) {
-                const int4 o = __ldg(g.root + 2 + k);
-                if (o.x == kx && o.y == ky && o.z == kz) {
-                    r.i5 = k;
-                    lvl = 5;
-                    break;
-                }
-            }
+        const uint32_t k = root_find(g, x, y, z);
+        if (k != kNoNode) {
+            r.i5 = k;
+            lvl = 5;
         }
     }
     if (lvl == 5) {  // get_vdb_leaf_from_node5 (:415-444)
@@ -492,10 +499,111 @@ __device__ __forceinline__ uint32_t pack_rgba(F3 c) {
     return unorm8(c.x) | (unorm8(c.y) << 8) | (unorm8(c.z) << 16) | (255u << 24);
 }
 
-__device__ __forceinline__ void store_hit(wx_hit *h, F3 p, float t, uint32_t node, uint32_t info, uint32_t shadow) {
+__device__ __forceinline__ void store_hit(wx_hit *h, F3 p, float t, uint32_t node, uint32_t info, uint32_t shadow,
+                                          uint32_t reserved = 0u) {
     uint4 *q = reinterpret_cast<uint4 *>(h);
     q[0] = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), __float_as_uint(p.z), __float_as_uint(t));
-    q[1] = make_uint4(node, info, shadow, 0u);
+    q[1] = make_uint4(node, info, shadow, reserved);
+}
+
+// ---------------------------------------------------------------------------
+// Zero-crossing hit mode (WX_MODE_SURFACE). An extension with no counterpart
+// in the reference, specified by the oracle's surf_* functions, which this
+// code follows operation for operation.
+// ---------------------------------------------------------------------------
+constexpr float kSurfH = 0.25f;   // sample spacing along the ray, voxels
+constexpr uint32_t kSurfN = 64u;  // samples
+
+// Level-set value of voxel (i, j, k): the leaf value, -band inside an active
+// tile (slot word 0), +band anywhere else.
+__device__ __forceinline__ float surf_phi(const DevGrid &g, int i, int j, int k) {
+    const uint32_t n5 = root_find(g, i, j, k);
+    if (n5 == kNoNode) return g.band;
+    const uint32_t w5 = __ldg(g.slot5 + ((n5 << 15) | ((((uint32_t)i >> 7) & 31u) << 10) |
+                                         ((((uint32_t)j >> 7) & 31u) << 5) | (((uint32_t)k >> 7) & 31u)));
+    if (!(w5 & kChild)) return w5 == 0u ? -g.band : g.band;
+    const uint32_t w4 = __ldg(g.slot4 + (((w5 & ~kChild) << 12) | ((((uint32_t)i >> 3) & 15u) << 8) |
+                                         ((((uint32_t)j >> 3) & 15u) << 4) | (((uint32_t)k >> 3) & 15u)));
+    if (!(w4 & kChild)) return w4 == 0u ? -g.band : g.band;
+    return __ldg(g.values + (((w4 & ~kChild) << 9) | (((uint32_t)i & 7u) << 6) | (((uint32_t)j & 7u) << 3) |
+                             ((uint32_t)k & 7u)));
+}
+
+__device__ __forceinline__ float lerpf(float a, float b, float t) { return a + t * (b - a); }
+
+// Corner values of the cell of q (corner n = dx << 2 | dy << 1 | dz) and q's
+// position inside it.
+__device__ __forceinline__ void surf_cell(const DevGrid &g, F3 q, float c[8], float f[3]) {
+    const float fx = floorf(q.x), fy = floorf(q.y), fz = floorf(q.z);
+    const int i = __float2int_rd(q.x), j = __float2int_rd(q.y), k = __float2int_rd(q.z);
+    f[0] = q.x - fx;
+    f[1] = q.y - fy;
+    f[2] = q.z - fz;
+#pragma unroll
+    for (int n = 0; n < 8; n++) c[n] = surf_phi(g, i + (n >> 2), j + ((n >> 1) & 1), k + (n & 1));
+}
+
+__device__ __forceinline__ float surf_interp(const float c[8], const float f[3]) {
+    const float a00 = lerpf(c[0], c[4], f[0]), a10 = lerpf(c[2], c[6], f[0]);
+    const float a01 = lerpf(c[1], c[5], f[0]), a11 = lerpf(c[3], c[7], f[0]);
+    return lerpf(lerpf(a00, a10, f[1]), lerpf(a01, a11, f[1]), f[2]);
+}
+
+__device__ __forceinline__ F3 surf_gradient(const float c[8], const float f[3]) {
+    const float gx = lerpf(lerpf(c[4] - c[0], c[6] - c[2], f[1]), lerpf(c[5] - c[1], c[7] - c[3], f[1]), f[2]);
+    const float gy = lerpf(lerpf(c[2] - c[0], c[6] - c[4], f[0]), lerpf(c[3] - c[1], c[7] - c[5], f[0]), f[2]);
+    const float gz = lerpf(lerpf(c[1] - c[0], c[5] - c[4], f[0]), lerpf(c[3] - c[2], c[7] - c[6], f[0]), f[1]);
+    return f3(gx, gy, gz);
+}
+
+__device__ __forceinline__ float surf_sample(const DevGrid &g, F3 eye, F3 dir, float t) {
+    float c[8], f[3];
+    surf_cell(g, f3(eye.x + t * dir.x, eye.y + t * dir.y, eye.z + t * dir.z), c, f);
+    return surf_interp(c, f);
+}
+
+// Search from t_hit - 1 (the HDDA hit's t); true with t*, the sample index and
+// the normal when phi changes sign within kSurfN samples.
+__device__ __noinline__ bool surf_search(const DevGrid &g, F3 eye, F3 dir, float t_hit, float *ts, uint32_t *ks,
+                                         F3 *N) {
+    if (!g.values) return false;
+    float t0 = t_hit - 1.0f;
+    if (!(t0 > 0.0f)) t0 = 0.0f;
+    float prev = surf_sample(g, eye, dir, t0);
+    bool found = false;
+    if (prev <= 0.0f) {
+        *ts = t0;
+        *ks = 0;
+        found = true;
+    } else {
+        for (uint32_t k = 1; k < kSurfN; k++) {
+            const float tk = t0 + __uint2float_rn(k) * kSurfH;
+            const float ph = surf_sample(g, eye, dir, tk);
+            if (ph <= 0.0f) {
+                const float tp = t0 + __uint2float_rn(k - 1u) * kSurfH;
+                *ts = tp + kSurfH * __fdiv_rn(prev, prev - ph);
+                *ks = k;
+                found = true;
+                break;
+            }
+            prev = ph;
+        }
+    }
+    if (!found) return false;
+    float c[8], f[3];
+    surf_cell(g, f3(eye.x + *ts * dir.x, eye.y + *ts * dir.y, eye.z + *ts * dir.z), c, f);
+    const F3 gr = surf_gradient(c, f);
+    *N = dot3(gr, gr) == 0.0f ? -dir : normalize3(gr);
+    return true;
+}
+
+// Mode 5 colour: mode 3's I_a + I_d with normal N, no shadow ray.
+__device__ __forceinline__ F3 surface_colour(const wx_state_uniform &s, F3 N) {
+    const F3 sun = f3(s.sun_dir[0], s.sun_dir[1], s.sun_dir[2]);
+    const F3 sc = f3(s.sun_color[0], s.sun_color[1], s.sun_color[2]);
+    const float LN = pmax(0.0f, s.sun_color[3] * dot3(-sun, N));
+    const F3 I_d = ((kKd * sc) * f3(0.4f, 0.2f, 0.2f)) * LN;
+    return ambient_colour() + I_d;
 }
 
 }  // namespace wxd

@@ -16,7 +16,9 @@ struct DevGrid {
     const uint32_t *slot4;   // N4 slot words
     const uint8_t *leaf;     // N3: one byte per voxel, 0 hit, 1..254 distance, 255 = see ovf
     const uint2 *ovf;        // (voxel key = leaf << 9 | offset, distance), sorted by key
+    const float *values;     // level-set value per leaf voxel (zero-crossing mode), or null
     uint32_t n5, n_ovf;
+    float band;              // value of voxels outside leaves (+band; -band in active tiles)
 };
 
 // One frame of one grid: the unit the persistent kernels draw ray tiles from.
@@ -43,8 +45,12 @@ cudaError_t init_device_tables();
 int max_blocks_per_sm(int kernel, bool batched, int warps_per_block);
 cudaError_t launch_pixel(const Job &job, const Tuning &t, cudaStream_t st);
 cudaError_t launch_persistent(const Job &job, uint32_t *ctr, const Tuning &t, int num_sms, cudaStream_t st);
+// all: some job renders mode 4 or 5 (the kernels compiled for every mode).
 cudaError_t launch_batched(const Job *jobs_dev, uint32_t njobs, uint32_t total_tiles, uint32_t *ctr,
-                           const Tuning &t, int num_sms, cudaStream_t st);
+                           const Tuning &t, int num_sms, bool all, cudaStream_t st);
+// Modes 4 (glossy) and 5 (zero crossing) need the kernels compiled for every mode.
+bool all_modes(const wx_state_uniform &s);
+bool all_modes(const Job *jobs, size_t n);
 // Device pools and device of a grid handle (defined in api.cpp); false for NULL.
 bool grid_device_view(const wx_grid *grid, DevGrid *out, int *device);
 // Device index and SM count of a context (defined in api.cpp).

@@ -68,6 +68,16 @@ def spheres_topology(seed: int = 2) -> Topology:
     return Topology.spheres(2000, 4.0, 40.0, -1024.0, 1024.0, 3.0, seed)
 
 
+def sphere_values(topo: Topology) -> np.ndarray:
+    """Level-set values of sphere_topology's grid (zero-crossing mode)."""
+    return topo.sphere_values((0.0, 0.0, 0.0), 64.0, 3.0)
+
+
+def spheres_values(topo: Topology, seed: int = 2) -> np.ndarray:
+    """Level-set values of spheres_topology's grid (zero-crossing mode)."""
+    return topo.spheres_values(2000, 4.0, 40.0, -1024.0, 1024.0, 3.0, seed)
+
+
 def noise_topology(seed: int = 3) -> Topology:
     return Topology.noise_leaves(-2048, 4096, 0.02, 0.5, seed)
 
