@@ -519,6 +519,27 @@ def main():
                "h2d_bytes_per_step": 256 * len(frames), "d2h_bytes_per_step": W_ * H_ * 4 * len(frames),
                "ms_per_step": em}
 
+    # Batched vs plain on the same frames: all of them in one persistent launch (wx_render_batch),
+    # which removes the per-frame launch tails. `value` stays the plain per-frame figure.
+    same_batched = None
+    if not args.no_batched:
+        fr = [(grid, st, W_, H_, o, None) for st, o in zip(states, outs)]
+        for _ in range(args.warmup):
+            ctx.render_batch(fr, stream=sh)
+        bm = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.render_batch(fr, stream=sh)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            bm.append(e0.elapsed_time(e1))
+        b_ms = max_over_ranks(statistics.mean(bm), dist, dev)
+        same_batched = {"value": replica_throughput(rays_step, world, b_ms), "unit": "Grays/s", "ms_per_step": b_ms,
+                        "launches_per_step": 1, "speedup_over_plain": ms / b_ms,
+                        "note": f"the same {len(frames)} frames in one persistent launch"}
+
     # Mode 3 traces one shadow ray per lit hit inside the same launches; they are not in `value`.
     # Counted from the hit records of one untimed render of each frame.
     shadow = None
@@ -611,7 +632,7 @@ def main():
                        "autotune": tuned and {"table [kernel, tile_w, warps/block, ms for 4 frames]": tuned["table"],
                                               "seconds": tuned["seconds"]}},
             "frame_latency_ms": {"p50": p50, "p99": p99},
-            "batched": batched, "shadow_rays": shadow, "surface": surface,
+            "batched_same_frames": same_batched, "batched": batched, "shadow_rays": shadow, "surface": surface,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "gpu_launches": len(frames) * args.steps,
             "clocks": clk.summary(),
