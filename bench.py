@@ -159,7 +159,8 @@ def sample_tiles(frame, fraction, rng):
 def oracle_sample(view, frames, fraction, nthreads, seed=5, stats=False):
     """Render a random `fraction` of the 8x4 tiles of every frame on the CPU oracle.
 
-    Returns (rays, seconds, mean node-visit bytes per primary ray incl. its shadow ray)."""
+    Returns (rays, seconds, mean node-visit bytes per primary ray incl. its shadow ray, grazing
+    fraction of the primary rays); the last two only with stats=True."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import ctypes as C
 
@@ -169,7 +170,7 @@ def oracle_sample(view, frames, fraction, nthreads, seed=5, stats=False):
     L = orc.lib()
     s, keep = orc._view_struct(view)
     rng = np.random.default_rng(seed)
-    rays, secs, byte_sum = 0, 0.0, 0.0
+    rays, secs, byte_sum, grazing = 0, 0.0, 0.0, 0
     for fr in frames:
         st = fr.state()
         sb = C.create_string_buffer(wx.state_bytes(st), 256)
@@ -190,8 +191,9 @@ def oracle_sample(view, frames, fraction, nthreads, seed=5, stats=False):
                 x0, y0 = (t % (fr.width // 8)) * 8, (t // (fr.width // 8)) * 4
                 m[y0:y0 + 4, x0:x0 + 8] = True
             byte_sum += float(stt["bytes"][m].sum() + stt["shadow_bytes"][m].sum())
+            grazing += int(stt["grazing"][m].sum())
     del keep
-    return rays, secs, (byte_sum / rays if stats else None)
+    return rays, secs, (byte_sum / rays if stats else None), (grazing / rays if stats else None)
 
 
 def run_reference(args, wl_name):
@@ -212,7 +214,7 @@ def run_reference(args, wl_name):
         oracle_sample(view, wl.frames[:1], frac / 4, nthreads, seed=99)
     times, rays_tot = [], 0
     for k in range(args.steps):
-        rays, secs, _ = oracle_sample(view, wl.frames, frac, nthreads, seed=100 + k)
+        rays, secs, _, _ = oracle_sample(view, wl.frames, frac, nthreads, seed=100 + k)
         times.append(secs)
         rays_tot += rays
     total = sum(times)
@@ -593,16 +595,20 @@ def main():
         sphere_grid.release()
 
     # roofline + CPU baseline from the oracle on a sample of the same tiles (rank 0)
-    roof, cpu = None, None
+    roof, cpu, graze = None, None, None
     kernel_name = "k_persistent" if ctx.tuning["kernel"] == 0 else "k_pixel"  # after autotuning
     if rank == 0:
         peak, peak_kind = hbm_peak()
         view = topo.view()
         nthreads = os.cpu_count() or 1
-        rays_s, secs, bpr = oracle_sample(view, frames, args.cpu_fraction, nthreads, seed=5, stats=True)
+        rays_s, secs, bpr, grazing = oracle_sample(view, frames, args.cpu_fraction, nthreads, seed=5, stats=True)
         launch_avg_ms = statistics.mean(launch_ms)
         bytes_launch = bpr * frames[0].rays
         achieved = bytes_launch / (launch_avg_ms / 1e3) / 1e9
+        graze = {"fraction": grazing, "rays": rays_s,
+                 "note": "primary rays of the CPU sample with a step whose winning tMax is within 1 ulp of "
+                         "another or that lands within 1 ulp of a cell boundary; the kernels match the oracle "
+                         "on them bit for bit (parity tests)"}
         l2 = l2_copy_peak(dev)
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": profiled_traffic(kernel_name, args.workload), "peak_kind": peak_kind,
@@ -614,7 +620,7 @@ def main():
             cpu = {"value": rays_s / secs / 1e9, "unit": "Grays/s", "cores": nthreads, "kind": "port",
                    "sample": f"{args.cpu_fraction:.4f} of the 8x4 tiles of each of the {len(frames)} frames "
                              f"({rays_s} rays), C restatement of raycast.comp.wgsl, {nthreads} threads"}
-            r1, s1, _ = oracle_sample(view, frames, args.cpu_fraction / 16, 1, seed=6)
+            r1, s1, _, _ = oracle_sample(view, frames, args.cpu_fraction / 16, 1, seed=6)
             cpu["single_thread"] = {"value": r1 / s1 / 1e9, "unit": "Grays/s", "cores": 1,
                                     "sample": f"{args.cpu_fraction / 16:.5f} of the tiles ({r1} rays)"}
         del view
@@ -633,7 +639,7 @@ def main():
                                               "seconds": tuned["seconds"]}},
             "frame_latency_ms": {"p50": p50, "p99": p99},
             "batched_same_frames": same_batched, "batched": batched, "shadow_rays": shadow, "surface": surface,
-            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "grazing_rays": graze,
             "gpu_launches": len(frames) * args.steps,
             "clocks": clk.summary(),
         }
