@@ -196,6 +196,11 @@ def oracle_sample(view, frames, fraction, nthreads, seed=5, stats=False):
     return rays, secs, (byte_sum / rays if stats else None), (grazing / rays if stats else None)
 
 
+def workload_label(name: str, frames) -> str:
+    """config.workload of both arms: the workload and its frames."""
+    return f"{name}: {len(frames)} x {frames[0].width}x{frames[0].height} frames, plain per-frame launches"
+
+
 def run_reference(args, wl_name):
     """--impl reference: the reference algorithm on the host cores (rank 0 only)."""
     rank = int(os.environ.get("RANK", "0"))
@@ -224,7 +229,9 @@ def run_reference(args, wl_name):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": wl_name, "frames": len(wl.frames), "parallelism": "cpu-threads"},
+        "config": {"workload": workload_label(wl_name, wl.frames),
+                   "grid": dict(zip(("n5", "n4", "n3"), topo.counts), active_voxels=topo.active_voxels),
+                   "render_mode": wl.frames[0].mode, "parallelism": f"cpu-threads x{nthreads}"},
         "cpu_baseline": {"value": value, "unit": "Grays/s", "cores": nthreads, "kind": "port",
                          "sample": f"{frac:.4f} of the 8x4 tiles of each of the {len(wl.frames)} frames per step, "
                                    f"C restatement of raycast.comp.wgsl (oracle/), {nthreads} threads"},
@@ -630,7 +637,7 @@ def main():
             "metric": "primary_ray_grays_per_s", "value": value, "unit": "Grays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"{args.workload}: {len(frames)} x {W_}x{H_} frames, plain per-frame launches",
+            "config": {"workload": workload_label(args.workload, frames),
                        "grid": {k: info[k] for k in ("n5", "n4", "n3", "active_voxels", "device_bytes")},
                        "grid_build_s": {"host_sdf": round(t_build, 3), "gpu_sdf": round(t_build_gpu, 3)},
                        "render_mode": frames[0].mode, "l2": "flushed between steps (512 MB write)",
