@@ -49,10 +49,10 @@ __device__ __forceinline__ float sign11(float x) { return x < 0.0f ? -1.0f : 1.0
 // size*step01 - mod, where +0 and -0 give the same value). Other cases
 // (dist >= 4096, or a coordinate with |p| < 2^-64, where q0 could underflow)
 // take __fdiv_rn.
-__device__ __forceinline__ float rcp_size(uint32_t dist, int sk, bool *fast) {
+__device__ __forceinline__ float rcp_size(uint32_t dist, uint32_t rbits, bool *fast) {
     *fast = dist < kRcp;
     const float r = __ldg(&g_rcp[*fast ? dist : 1u]);
-    return r * __int_as_float((127 - sk) << 23);  // sk <= 12
+    return r * __uint_as_float(rbits);  // rbits = 2^-sk, sk <= 12
 }
 __device__ __forceinline__ float div_fast(float p, float size, float y) {
     const float q0 = p * y;
@@ -193,6 +193,9 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     else if (r.np >= 1 && d < 4096u) lvl = 5;
     else lvl = 0;
     uint32_t dist = 1;
+    // 2^sk and 2^-sk as float bits, sk = log2 of the size scale of the level
+    // that resolves the voxel (:105-112): 12, 7, 3, 0 for 0..3 cached parents.
+    uint32_t sbits = (127u + 12u) << 23, rbits = (127u - 12u) << 23;
     if (lvl == 0) {  // get_vdb_leaf_from_nothing (:398-413): the N5 whose origin is floor(p) & ~4095
         r.np = 0;
         const uint32_t k = root_find(g, x, y, z);
@@ -206,6 +209,8 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
                              (((uint32_t)z >> 7) & 31u);
         const uint32_t w = __ldg(g.slot5 + ((r.i5 << 15) | off));
         r.np = 1;
+        sbits = (127u + 7u) << 23;
+        rbits = (127u - 7u) << 23;
         if (w & kChild) {
             r.i4 = w & ~kChild;
             lvl = 4;
@@ -218,6 +223,8 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
                              (((uint32_t)z >> 3) & 15u);
         const uint32_t w = __ldg(g.slot4 + ((r.i4 << 12) | off));
         r.np = 2;
+        sbits = (127u + 3u) << 23;
+        rbits = (127u - 3u) << 23;
         if (w & kChild) {
             r.i3 = w & ~kChild;
             lvl = 3;
@@ -230,16 +237,16 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
         dist = __ldg(g.leaf + key);
         if (dist == 255u) dist = leaf_overflow(g, key);
         r.np = 3;
+        sbits = rbits = 127u << 23;
     }
     if (dist == 0u) return 0u;
     const float apx = fabsf(r.px), apy = fabsf(r.py), apz = fabsf(r.pz);
     // any(4096 < |p|); a NaN coordinate compares false, and fmaxf skips NaN.
     if (4096.0f < fmaxf(fmaxf(apx, apy), apz)) return 1u;
     // size = f32(dist) * scale[by num_parents] (:105-112); log2 scale by np = 12, 7, 3, 0.
-    const int sk = (0x037C >> (r.np << 2)) & 15;
-    const float size = __uint2float_rn(dist) * __int_as_float((127 + sk) << 23);
+    const float size = __uint2float_rn(dist) * __uint_as_float(sbits);
     bool fast;
-    const float ys = rcp_size(dist, sk, &fast);
+    const float ys = rcp_size(dist, rbits, &fast);
     // tMax = idir * (size * step01 - (p - size * floor(p / size)))  (:78-80, :114)
     float tx, ty, tz;
     // The fast quotient needs every coordinate of magnitude >= 2^-64 (a zero
