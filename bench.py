@@ -473,7 +473,8 @@ def main():
         t0 = time.perf_counter()
         tuned = ctx.autotune([(grid, st, W_, H_, o, None) for st, o in list(zip(states, outs))[:4]], reps=2)
         tuned["seconds"] = time.perf_counter() - t0
-        tuned["table"] = [[c["kernel"], c["tile_width"], c["warps_per_block"], round(ms, 4)] for c, ms in tuned["table"]]
+        tuned["table"] = [[c["kernel"], c["tile_width"], c["warps_per_block"], c["blocks_per_sm"], round(ms, 4)]
+                          for c, ms in tuned["table"]]
         log(f"[bench] autotune -> {tuned['best']} in {tuned['seconds']:.1f}s")
     for _ in range(args.warmup):
         step()
@@ -642,7 +643,8 @@ def main():
                        "grid_build_s": {"host_sdf": round(t_build, 3), "gpu_sdf": round(t_build_gpu, 3)},
                        "render_mode": frames[0].mode, "l2": "flushed between steps (512 MB write)",
                        "parallelism": f"replicas x{world}", "tuning": ctx.tuning,
-                       "autotune": tuned and {"table [kernel, tile_w, warps/block, ms for 4 frames]": tuned["table"],
+                       "autotune": tuned and {"table [kernel, tile_w, warps/block, blocks/SM (0 = all that fit), ms for 4 frames]":
+                                              tuned["table"],
                                               "seconds": tuned["seconds"]}},
             "frame_latency_ms": {"p50": p50, "p99": p99},
             "batched_same_frames": same_batched, "batched": batched, "shadow_rays": shadow, "surface": surface,

@@ -184,7 +184,8 @@ int wx_ctx_get_tuning(const wx_ctx *ctx, wx_tuning *tuning);
  * frame with each candidate tuning, reps times after one warm-up pass, timing
  * with CUDA events, and installs the fastest on the context. candidates NULL
  * (ncand ignored) uses the built-in set: both kernels x tile widths {4, 8, 16}
- * x {2, 4, 8} warps per block. times_ms (ncand or 18 entries, may be NULL)
+ * x {2, 4, 8} warps per block, plus the persistent kernel at 4 blocks of 4
+ * warps per SM (tile widths 4, 8). times_ms (ncand or 20 entries, may be NULL)
  * receives each candidate's mean time for all frames. */
 int wx_autotune(wx_ctx *ctx, const wx_frame *frames, uint32_t n, const wx_tuning *candidates, uint32_t ncand,
                 uint32_t reps, wx_tuning *best, double *times_ms);

@@ -411,6 +411,8 @@ int wx_autotune(wx_ctx *ctx, const wx_frame *frames, uint32_t n, const wx_tuning
         for (int kernel : {0, 1})
             for (int tw : {4, 8, 16})
                 for (int wpb : {2, 4, 8}) cand.push_back(wx_tuning{kernel, wpb, 0, tw});
+        // Occupancy of the persistent kernel: fewer resident warps than fit (16 per SM).
+        for (int tw : {4, 8}) cand.push_back(wx_tuning{0, 4, 4, tw});
     }
     if (cand.empty()) return fail(ctx, WX_ERR_INVALID, "wx_autotune: no candidates");
     for (uint32_t i = 0; i < n; i++)
