@@ -347,6 +347,14 @@ typedef struct wx_vdb_info {
     char grid_name[64];
 } wx_vdb_info;
 int wx_vdb_read_topology(const char *path, const char *grid_name, wx_topology **out, wx_vdb_info *info);
+/* The grid's leaf values (the tree-data section, read.rs:571-629) in the layout
+ * of wx_grid_set_values: n3 * 512 floats in DFS leaf order (half-float files
+ * converted). Inactive voxels the file leaves implicit read +background, or
+ * -background where the node's metadata says so (the OpenVDB format's rule; the
+ * reference reader leaves them zero). values NULL: only *count (n3 * 512) and
+ * *background are returned. */
+int wx_vdb_read_leaf_values(const char *path, const char *grid_name, float *values, uint64_t capacity,
+                            uint64_t *count, float *background);
 
 /* ---- synthetic grids (seeded; f32 narrow-band level sets use value = signed distance) ---- */
 /* Voxels with |(|ijk - c| - r)| < band are active. */

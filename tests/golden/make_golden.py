@@ -8,6 +8,8 @@ reference checkout's assets/ directory). For each fixture this writes
                        (masks/origins in DFS order) plus the file's
                        file_voxel_count metadata, which the reference's own test
                        (src/vdb/read.rs:733-807) compares with the voxel count;
+  <name>_values.npz    its leaf values (float16, as the half-float file stores them)
+                       and the grid's background, read by the product's reader;
   <name>_render.npz    oracle renders of that topology (uniform bytes, RGBA8 and
                        hit records) for a few cameras and modes.
 It also writes sphere64_render.npz (the 64-voxel sphere of the benchmark's small
@@ -59,6 +61,10 @@ def main(assets: Path) -> None:
         np.savez_compressed(HERE / f"{name}_topology.npz", **m,
                             file_voxel_count=np.array(meta["file_voxel_count"], np.int64),
                             file_version=np.array(meta["file_version"], np.int32))
+        vals, bg = wx.Topology.read_vdb_values(assets / f"{name}.vdb", f"ls_{name}")
+        half = vals.astype(np.float16)
+        assert np.array_equal(half.astype(np.float32), vals)  # half-float files: exact
+        np.savez_compressed(HERE / f"{name}_values.npz", values=half, background=np.float32(bg))
         view = orc.Tree.from_masks(m).view()
         np.savez_compressed(HERE / f"{name}_render.npz", **render_set(name, view))
         print(name, topo.counts, topo.active_voxels, meta)

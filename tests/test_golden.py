@@ -47,6 +47,35 @@ def test_reader_reproduces_frozen_topology(name):
         np.testing.assert_array_equal(got[k], m[k], err_msg=k)
 
 
+def frozen_values(name):
+    d = np.load(GOLDEN / f"{name}_values.npz")
+    return d["values"].astype(np.float32), float(d["background"])
+
+
+@pytest.mark.parametrize("name", ["cube", "icosahedron"])
+def test_reader_reproduces_frozen_values(name):
+    """Leaf values of the tree-data section (read.rs:571-629), half floats converted exactly."""
+    path = ASSETS / f"{name}.vdb"
+    if not path.exists():
+        pytest.skip("reference assets not present on this machine")
+    vals, bg = wx.Topology.read_vdb_values(path, f"ls_{name}")
+    want, want_bg = frozen_values(name)
+    assert bg == want_bg
+    np.testing.assert_array_equal(vals, want)
+
+
+@pytest.mark.parametrize("name", ["cube", "icosahedron"])
+def test_frozen_values_are_a_level_set(name):
+    """Active voxels lie inside the narrow band; inactive ones hold +-background (outside/inside)."""
+    m, _ = frozen_masks(name)
+    v, bg = frozen_values(name)
+    v = v.reshape(-1, 512)
+    bits = np.unpackbits(m["vals3"].view(np.uint8), bitorder="little").reshape(-1, 512).astype(bool)
+    assert (np.abs(v[bits]) <= bg).all() and (np.abs(v[bits]) < bg).mean() > 0.999
+    assert np.array_equal(np.abs(v[~bits]), np.full((~bits).sum(), bg, np.float32))
+    assert 0.3 < (v[~bits] < 0).mean() < 0.6  # both sides of the surface are present
+
+
 def test_reader_rejects_bad_files(tmp_path):
     p = tmp_path / "bad.vdb"
     p.write_bytes(b"\x00" * 64)

@@ -61,3 +61,25 @@ def test_without_values_no_crossing_is_found():
     st0 = wx.state_build(eye=(0, 0, 200), target=(0, 0, 0), aspect=1.0, fovy=40.0, width=64.0, mode=0)
     rgba0, _, _ = orc.render(view, wx.state_bytes(st0), 64, 64, nthreads=4, hits=True)
     np.testing.assert_array_equal(rgba, rgba0)  # mode 0's colour where no crossing is found
+
+
+def test_crossings_on_the_cube_fixture():
+    """The reference's cube level set with its own values: crossings are found for almost all HDDA
+    hits, a little beyond them (the band is 3 voxels wide), with axis-aligned normals on the faces."""
+    from pathlib import Path
+
+    golden = Path(__file__).resolve().parent / "golden"
+    d = np.load(golden / "cube_topology.npz")
+    m = {k: d[k] for k in ("kids5", "vals5", "kids4", "vals4", "vals3", "origins")}
+    vd = np.load(golden / "cube_values.npz")
+    view = orc.Tree.from_masks(m).view()
+    view["values"], view["band"] = vd["values"].astype(np.float32), float(vd["background"])
+    st = wx.state_build(eye=(0.5, 0.5, 260.0), target=(0, 0, 0), aspect=1.0, fovy=40.0, width=96.0, mode=5)
+    rgba, hits, _ = orc.render(view, wx.state_bytes(st), 96, 96, nthreads=8, hits=True)
+    f = wx.hit_fields(hits)
+    hit = f["state"] == 0
+    found = (hits["shadow"] & 1) == 1
+    assert hit.sum() > 1000 and found[hit].mean() > 0.95
+    ts = hits["reserved"].view(np.float32)
+    dt = ts[found] - hits["t"][found]
+    assert (dt >= -1.0).all() and (dt < 8.0).all()

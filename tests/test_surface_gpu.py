@@ -77,3 +77,26 @@ def test_spheres_1080p_surface_sampled_tiles(cuda_ctx):
             m[y0:y0 + 4, x0:x0 + 8] = True
         compare_surface(rg, hg, ro, ho, f"spheres surface frame {k}", where=m)
         assert ((hg["shadow"][m] & 1) == 1).sum() > 1000
+
+
+@pytest.mark.parametrize("name", ["cube", "icosahedron"])
+def test_fixture_level_sets(cuda_ctx, name):
+    """The reference's own level sets with the values its files store (tests/golden)."""
+    from pathlib import Path
+
+    golden = Path(__file__).resolve().parent / "golden"
+    d = np.load(golden / f"{name}_topology.npz")
+    m = {k: d[k] for k in ("kids5", "vals5", "kids4", "vals4", "vals3", "origins")}
+    vd = np.load(golden / f"{name}_values.npz")
+    vals, bg = vd["values"].astype(np.float32), float(vd["background"])
+    topo = wx.Topology.from_masks(m)
+    view = topo.view()
+    view["values"], view["band"] = vals, bg
+    grid = cuda_ctx.build_grid(topo, gpu=True)
+    grid.set_values(vals, bg)
+    for eye in [(0.5, 0.5, 260.0), (180.0, 150.0, 240.0), (-230.0, -90.0, -170.0)]:
+        st = wx.state_build(eye=eye, target=(0, 0, 0), aspect=4 / 3, fovy=50.0, width=128.0, mode=5)
+        rg, hg = gpu_render(cuda_ctx, grid, st, 128, 96)
+        ro, ho = oracle_render(view, st, 128, 96)
+        compare_surface(rg, hg, ro, ho, f"{name} surface eye={eye}")
+        assert ((hg["shadow"] & 1) == 1).sum() > 500

@@ -90,6 +90,17 @@ class Topology:
                 "grid_name": info.grid_name.decode()}
         return Topology(out.value), meta
 
+    @staticmethod
+    def read_vdb_values(path, grid_name: Optional[str] = None) -> tuple:
+        """Leaf values of one grid of an OpenVDB file (n3 * 512 float32, wx_grid_set_values layout)
+        and the grid's background value."""
+        n, bg = C.c_uint64(), C.c_float()
+        g = grid_name.encode() if grid_name else None
+        check(lib().wx_vdb_read_leaf_values(str(path).encode(), g, None, 0, C.byref(n), C.byref(bg)))
+        out = np.empty(n.value, np.float32)
+        check(lib().wx_vdb_read_leaf_values(str(path).encode(), g, out.ctypes.data, out.size, C.byref(n), C.byref(bg)))
+        return out, bg.value
+
     @classmethod
     def from_voxels(cls, ijk) -> "Topology":
         a = np.ascontiguousarray(ijk, dtype=np.int32).reshape(-1, 3)

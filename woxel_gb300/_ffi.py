@@ -135,6 +135,7 @@ SIGNATURES = {
     "wx_gen_noise_leaves": (INT, [I32, U32, C.c_double, C.c_double, U64, INT, C.POINTER(P)]),
     "wx_orbit_eyes": (INT, [U32, F32, U64, P]),
     "wx_vdb_read_topology": (INT, [C.c_char_p, C.c_char_p, C.POINTER(P), C.POINTER(wx_vdb_info)]),
+    "wx_vdb_read_leaf_values": (INT, [C.c_char_p, C.c_char_p, P, U64, C.POINTER(C.c_uint64), C.POINTER(F32)]),
 }
 
 _lib = None

@@ -6,8 +6,10 @@
 // headers (:351-488). Only the topology is needed by the raycast pass: leaf
 // values never enter the march (a voxel hits by its value-mask bit), and the
 // reference sets LeafData::Value exactly where the topology's leaf mask is set
-// (read.rs:610-620). The tree-data section is therefore not parsed.
-// Blosc- or zip-compressed node headers are rejected (WX_ERR_UNSUPPORTED).
+// (read.rs:610-620). wx_vdb_read_topology therefore does not parse the
+// tree-data section; wx_vdb_read_leaf_values does (read_tree_data, :571-629),
+// for the zero-crossing mode's level-set values. Blosc- or zip-compressed data
+// is rejected (WX_ERR_UNSUPPORTED).
 
 #include <algorithm>
 #include <cstdio>
@@ -99,6 +101,19 @@ Meta read_metadata(Reader &r) {
     return m;
 }
 
+// IEEE binary16 -> binary32 (exact: every half is a float).
+float half_to_float(uint16_t h) {
+    const uint32_t s = (uint32_t)(h >> 15) << 31, e = (h >> 10) & 31u, m = h & 1023u;
+    if (e == 0) {
+        const float v = (float)m * 0x1p-24f;  // zero or subnormal
+        return s ? -v : v;
+    }
+    uint32_t bits = e == 31 ? (s | 0x7F800000u | (m << 13)) : (s | ((e + 112u) << 23) | (m << 13));
+    float f;
+    memcpy(&f, &bits, 4);
+    return f;
+}
+
 struct Grid {
     std::string name, type;
     uint64_t grid_pos = 0, block_pos = 0, end_pos = 0;
@@ -125,17 +140,63 @@ bool skip_compressed(Reader &r, uint32_t version, const Grid &g, size_t size, co
     return r.ok;
 }
 
-}  // namespace
-
-extern "C" int wx_vdb_read_topology(const char *path, const char *grid_name, wx_topology **out, wx_vdb_info *info) {
-    if (!path || !out) {
-        wx::set_thread_error("wx_vdb_read_topology: null argument");
-        return WX_ERR_INVALID;
+// Leaf buffers of the tree-data section (read_tree_data, read.rs:571-629, with
+// read_compressed, :378-488): per leaf, its value mask, then the values: a
+// metadata byte, up to two inactive values, an optional selection mask, and
+// either all 512 values or (active-mask compression) only the active ones, in
+// float or half. Inactive voxels get the inactive values; where the file gives
+// none they are +background, or -background for metadata 1 (NO_MASK_AND_MINUS_BG),
+// as the OpenVDB format defines them (the reference reader leaves them zero).
+bool read_leaf_values(Reader &r, uint32_t version, const Grid &g, float background, float *out) {
+    uint64_t vmask[8];
+    r.bytes(vmask, 64);
+    if (version < kNodeMaskCompression) {
+        r.skip(12);  // origin
+        if (r.get<uint8_t>() != 1) return r.fail("leaf with more than one buffer");
     }
+    uint8_t meta = 6;
+    if (version >= kNodeMaskCompression) meta = r.get<uint8_t>();
+    if (meta > 6) return r.fail("invalid node metadata");
+    float in0 = meta == 0 ? background : -background, in1 = background;
+    if (meta == 2 || meta == 4 || meta == 5) in0 = r.get<float>();
+    if (meta == 5) in1 = r.get<float>();
+    uint64_t sel[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (meta == 3 || meta == 4 || meta == 5) r.bytes(sel, 64);
+    size_t count = 512;
+    if ((g.compression & kActiveMask) && meta != 6 && version >= kNodeMaskCompression) {
+        count = 0;
+        for (uint64_t w : vmask) count += (size_t)__builtin_popcountll(w);
+    }
+    if (g.compression & (kBlosc | kZip)) return r.fail("blosc/zip-compressed grids are not supported");
+    float data[512];
+    if (g.meta.half) {
+        uint16_t h[512];
+        r.bytes(h, count * 2);
+        for (size_t i = 0; i < count; i++) data[i] = half_to_float(h[i]);
+    } else {
+        r.bytes(data, count * 4);
+    }
+    if (!r.ok) return false;
+    if (count == 512) {
+        memcpy(out, data, sizeof data);
+    } else {
+        size_t k = 0;
+        for (uint32_t i = 0; i < 512; i++) {
+            const bool act = (vmask[i >> 6] >> (i & 63)) & 1u, s1 = (sel[i >> 6] >> (i & 63)) & 1u;
+            out[i] = act ? data[k++] : (s1 ? in1 : in0);
+        }
+    }
+    return true;
+}
+
+// Parses one grid: the topology, and with values != nullptr also the leaf values
+// (n3 * 512 floats in DFS leaf order, the layout of wx_grid_set_values).
+int parse(const char *path, const char *grid_name, wx_topology **out, wx_vdb_info *info,
+          std::vector<float> *values, float *bg_out, const char *who) {
     Reader r;
     r.f = fopen(path, "rb");
     if (!r.f) {
-        wx::set_thread_error(std::string("wx_vdb_read_topology: cannot open ") + path);
+        wx::set_thread_error(std::string(who) + ": cannot open " + path);
         return WX_ERR_INVALID;
     }
     struct Closer {
@@ -143,7 +204,7 @@ extern "C" int wx_vdb_read_topology(const char *path, const char *grid_name, wx_
         ~Closer() { fclose(f); }
     } closer{r.f};
     auto bad = [&](int code, const std::string &m) {
-        wx::set_thread_error("wx_vdb_read_topology: " + m);
+        wx::set_thread_error(std::string(who) + ": " + m);
         return code;
     };
     // Archive header (read.rs:62-121).
@@ -196,7 +257,8 @@ extern "C" int wx_vdb_read_topology(const char *path, const char *grid_name, wx_
     else return bad(WX_ERR_UNSUPPORTED, "unsupported transform " + map);
     // Tree topology (read.rs:270-349).
     if (r.get<uint32_t>() != 1) return bad(WX_ERR_UNSUPPORTED, "multi-buffer trees");
-    r.get<uint32_t>();  // background
+    const float background = r.get<float>();
+    if (bg_out) *bg_out = background;
     const uint32_t ntiles = r.get<uint32_t>(), nnode5 = r.get<uint32_t>();
     r.skip((long)ntiles * (12 + 4 + 1));  // root tiles are invisible to masks()/origins()
     struct N4 {
@@ -209,6 +271,7 @@ extern "C" int wx_vdb_read_topology(const char *path, const char *grid_name, wx_
         std::vector<N4> kids;
     };
     std::map<wx::I3, N5> n5s;  // sorted root keys, as masks()/origins() iterate them
+    std::vector<wx::I3> file_order;  // the order the tree-data section lists the leaves in
     for (uint32_t i = 0; i < nnode5 && r.ok; i++) {
         N5 n;
         for (int a = 0; a < 3; a++) n.o[a] = wx::node_origin(r.get<int32_t>(), wx::kN5Total);
@@ -244,12 +307,15 @@ extern "C" int wx_vdb_read_topology(const char *path, const char *grid_name, wx_
             n.kids.push_back(std::move(c));
         }
         if (n5s.count(n.o)) return bad(WX_ERR_INVALID, "duplicate root key");
+        file_order.push_back(n.o);
         n5s.emplace(n.o, std::move(n));
     }
     if (!r.ok) return bad(r.err.find("supported") != std::string::npos ? WX_ERR_UNSUPPORTED : WX_ERR_INVALID, r.err);
     // masks()/origins() in DFS order (vdb345.rs:108-161).
     std::vector<uint32_t> k5, v5, k4, v4, v3;
     std::vector<int32_t> org;
+    std::map<wx::I3, size_t> first_leaf;  // DFS index of each N5's first leaf
+    size_t nleaves = 0;
     auto put = [](std::vector<uint32_t> &dst, const std::vector<uint64_t> &src) {
         for (uint64_t w : src) {
             dst.push_back((uint32_t)w);
@@ -257,6 +323,7 @@ extern "C" int wx_vdb_read_topology(const char *path, const char *grid_name, wx_
         }
     };
     for (auto &kv : n5s) {
+        first_leaf[kv.first] = nleaves;
         put(k5, kv.second.kid);
         put(v5, kv.second.val);
         org.insert(org.end(), {kv.first[0], kv.first[1], kv.first[2], 0});
@@ -264,11 +331,30 @@ extern "C" int wx_vdb_read_topology(const char *path, const char *grid_name, wx_
             put(k4, c.kid);
             put(v4, c.val);
             for (auto &m : c.leaves) put(v3, m);
+            nleaves += c.leaves.size();
         }
     }
-    const int rc = wx_topology_from_masks(k5.data(), v5.data(), n5s.size(), k4.data(), v4.data(), k4.size() / 128,
-                                          v3.data(), v3.size() / 16, org.data(), 4, out);
-    if (rc != WX_OK) return rc;
+    if (values) {  // tree data (read.rs:571-629): leaf buffers in the topology's file order
+        try {
+            values->assign(nleaves * 512, 0.0f);
+        } catch (...) {
+            return bad(WX_ERR_OOM, "host allocation failed");
+        }
+        r.seek(g.block_pos);
+        for (const wx::I3 &o : file_order) {
+            size_t leaf = first_leaf[o];
+            for (auto &c : n5s[o].kids)
+                for (size_t j = 0; j < c.leaves.size() && r.ok; j++, leaf++)
+                    if (!read_leaf_values(r, version, g, background, values->data() + leaf * 512)) break;
+        }
+        if (!r.ok)
+            return bad(r.err.find("supported") != std::string::npos ? WX_ERR_UNSUPPORTED : WX_ERR_INVALID, r.err);
+    }
+    if (out) {
+        const int rc = wx_topology_from_masks(k5.data(), v5.data(), n5s.size(), k4.data(), v4.data(), k4.size() / 128,
+                                              v3.data(), v3.size() / 16, org.data(), 4, out);
+        if (rc != WX_OK) return rc;
+    }
     if (info) {
         memset(info, 0, sizeof *info);
         info->file_version = version;
@@ -276,6 +362,36 @@ extern "C" int wx_vdb_read_topology(const char *path, const char *grid_name, wx_
         info->half_float = g.meta.half ? 1u : 0u;
         info->file_voxel_count = g.meta.voxel_count;
         snprintf(info->grid_name, sizeof info->grid_name, "%s", g.name.c_str());
+    }
+    return WX_OK;
+}
+
+}  // namespace
+
+extern "C" int wx_vdb_read_topology(const char *path, const char *grid_name, wx_topology **out, wx_vdb_info *info) {
+    if (!path || !out) {
+        wx::set_thread_error("wx_vdb_read_topology: null argument");
+        return WX_ERR_INVALID;
+    }
+    return parse(path, grid_name, out, info, nullptr, nullptr, "wx_vdb_read_topology");
+}
+
+extern "C" int wx_vdb_read_leaf_values(const char *path, const char *grid_name, float *values, uint64_t capacity,
+                                       uint64_t *count, float *background) {
+    if (!path || !count) {
+        wx::set_thread_error("wx_vdb_read_leaf_values: null argument");
+        return WX_ERR_INVALID;
+    }
+    std::vector<float> v;
+    const int rc = parse(path, grid_name, nullptr, nullptr, &v, background, "wx_vdb_read_leaf_values");
+    if (rc != WX_OK) return rc;
+    *count = v.size();
+    if (values) {
+        if (capacity < v.size()) {
+            wx::set_thread_error("wx_vdb_read_leaf_values: buffer too small");
+            return WX_ERR_INVALID;
+        }
+        memcpy(values, v.data(), v.size() * sizeof(float));
     }
     return WX_OK;
 }
