@@ -172,7 +172,10 @@ int wx_grid_read_pools(wx_ctx *ctx, const wx_grid *grid, uint32_t *slot5, uint32
 /* Renders the (8*floor(w/8)) x (4*floor(h/4)) pixels the reference dispatch
  * covers (wgpu_context.rs:281); other pixels are not written. rgba8 holds
  * w*h*4 bytes row-major; hits (w*h records) may be NULL. stream is a
- * cudaStream_t (NULL = legacy default stream). */
+ * cudaStream_t (NULL = legacy default stream). Outputs in device memory or in
+ * page-locked host memory are written by the kernel (complete when the stream
+ * is synchronised); pageable host outputs are staged on the device and copied
+ * back (complete on return). */
 int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, uint32_t width,
               uint32_t height, uint8_t *rgba8, wx_hit *hits, void *stream);
 

@@ -138,6 +138,27 @@ def test_host_buffers_match_device_buffers(cuda_ctx, sphere64):
     np.testing.assert_array_equal(hd.view(np.uint8), hh.view(np.uint8))
 
 
+def test_pinned_host_buffers_are_written_directly(cuda_ctx, sphere64):
+    """Page-locked host outputs (written by the kernel through their device alias) equal device outputs,
+    and pixels outside the dispatched region keep their contents."""
+    import torch
+
+    _, view, grid = sphere64
+    w, h = 101, 77
+    st = wx.state_build(eye=(100, 40, 120), target=(0, 0, 0), aspect=w / h, fovy=60.0, width=float(w), mode=3)
+    rd, hd = gpu_render(cuda_ctx, grid, st, w, h)
+    rgba = torch.full((h * w * 4,), 7, dtype=torch.uint8).pin_memory()
+    hits = torch.zeros(h * w * 32, dtype=torch.uint8).pin_memory()
+    cuda_ctx.render(grid, st, w, h, rgba, hits, stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    r = rgba.numpy().reshape(h, w, 4)
+    hh = hits.numpy().view(wx.HIT_DTYPE).reshape(h, w)
+    m = dispatch_mask(w, h)
+    np.testing.assert_array_equal(r[m], rd[m])
+    np.testing.assert_array_equal(hh[m].view(np.uint8), hd[m].view(np.uint8))
+    assert (r[~m] == 7).all()
+
+
 def test_ragged_resolution_leaves_border_untouched(cuda_ctx, sphere64):
     """Dispatch covers 8*floor(w/8) x 4*floor(h/4) pixels (wgpu_context.rs:281); the rest is not written."""
     _, view, grid = sphere64

@@ -102,6 +102,18 @@ bool device_accessible(const void *p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// The device-side address of page-locked host memory (cudaMallocHost,
+// cudaHostAlloc, cudaHostRegister), through which a kernel writes to the host
+// buffer directly; nullptr for pageable memory.
+void *pinned_device_alias(void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // A device allocation freed on scope exit (temporaries of wx_grid_build_gpu).
 struct DevBuf {
     void *p = nullptr;
@@ -816,11 +828,26 @@ int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, u
     if (ntiles == 0) return WX_OK;
     if ((uint64_t)width * height >= (1ull << 32)) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_render: frame too large");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const bool dev_rgba = device_accessible(rgba8);
-    const bool dev_hits = hits ? device_accessible(hits) : true;
-    const size_t npix = (size_t)width * height;
+    // Device memory and page-locked host memory are written by the kernel itself
+    // (page-locked memory through its device alias, over the host link while the
+    // march runs); pageable host memory goes through the context's staging buffer.
     uint32_t *out_rgba = reinterpret_cast<uint32_t *>(rgba8);
     wx_hit *out_hits = hits;
+    bool dev_rgba = device_accessible(rgba8);
+    bool dev_hits = hits ? device_accessible(hits) : true;
+    if (!dev_rgba) {
+        if (void *d = pinned_device_alias(rgba8)) {
+            out_rgba = static_cast<uint32_t *>(d);
+            dev_rgba = true;
+        }
+    }
+    if (!dev_hits) {
+        if (void *d = pinned_device_alias(hits)) {
+            out_hits = static_cast<wx_hit *>(d);
+            dev_hits = true;
+        }
+    }
+    const size_t npix = (size_t)width * height;
     if (!dev_rgba || !dev_hits) {
         const size_t need = npix * 4 + (hits ? npix * sizeof(wx_hit) + 256 : 0);
         if (need > ctx->stage_bytes) {
