@@ -156,8 +156,11 @@ int wx_grid_release(wx_ctx *ctx, wx_grid *grid);
 /* Attaches level-set values for WX_MODE_SURFACE: one float per leaf voxel
  * (n3 * 512, DFS leaf order, voxel order x<<6 | y<<3 | z), the signed distance
  * in voxel units, negative inside; voxels outside leaves read +band, or -band
- * inside an active tile. Replaces earlier values; freed with the grid. No
- * reference counterpart (the reference's raycast reads no values). */
+ * inside an active tile. Replaces earlier values; freed with the grid. Servers
+ * (wx_server_add_grid) and batch plans (wx_batch_create) keep the device view a
+ * grid had when they took it: attach values first. Not while a render of the
+ * grid is in flight. No reference counterpart (the reference's raycast reads no
+ * values). */
 int wx_grid_set_values(wx_ctx *ctx, wx_grid *grid, const float *values, float band);
 int wx_grid_get_info(const wx_grid *grid, wx_grid_info *out);
 /* Copies a grid's device pools to host memory; any pointer may be NULL.
@@ -278,7 +281,8 @@ typedef struct wx_server_stats {
 /* Creates the scheduler and allocates the output arena (budget minus the
  * grids added later is checked at admission). */
 int wx_server_create(wx_ctx *ctx, const wx_server_config *cfg, wx_server **out);
-/* Registers a resident grid; its device bytes count against the budget. */
+/* Registers a resident grid; its device bytes count against the budget. The
+ * server keeps the grid's device view as it is now (level-set values included). */
 int wx_server_add_grid(wx_server *srv, const wx_grid *grid, uint32_t *grid_id);
 /* Queues a request (never blocks on the GPU). WX_ERR_BUDGET if it could never fit. */
 int wx_server_submit(wx_server *srv, const wx_request *req, uint64_t *ticket);
