@@ -482,22 +482,33 @@ def main():
     if dist:
         dist.barrier()
 
-    step_ms, launch_ms = [], []
+    # Timed steps: one pair of events around the step's launches, which follow each
+    # other directly on the stream (back-to-back frames may overlap at their boundary).
+    step_ms = []
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
         for _ in range(args.steps):
             flush.zero_()  # L2 flush between timed iterations (outside the step's events)
-            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in frames]
-            step(ev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
             torch.cuda.synchronize()
-            lm = [a.elapsed_time(b) for a, b in ev]
-            launch_ms.extend(lm)
-            step_ms.append(ev[0][0].elapsed_time(ev[-1][1]))
+            step_ms.append(e0.elapsed_time(e1))
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
+    # Per-frame latency and launch duration: events around every launch (they separate
+    # the launches), on further steps of the same frames.
+    launch_ms = []
+    for _ in range(min(args.steps, 10)):
+        flush.zero_()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in frames]
+        step(ev)
+        torch.cuda.synchronize()
+        launch_ms.extend(a.elapsed_time(b) for a, b in ev)
     ms = max_over_ranks(statistics.mean(step_ms), dist, dev)
     rays_step = wl.rays
     value = replica_throughput(rays_step, world, ms)

@@ -80,6 +80,10 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
     }
     __syncwarp(act);
     const uint32_t pix = gy * J.width + gx;
+    // A programmatically dependent launch (launch_pixel) may run its march while
+    // the previous kernel of the stream finishes; its stores wait for that
+    // kernel to complete, so frames never overlap in memory. A no-op otherwise.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     J.rgba[pix] = pack_rgba(c);
     if (J.hits)
         store_hit(J.hits + pix, hit.p, dot3(hit.p - eye, dir), hit.node,
@@ -95,6 +99,8 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
 
 template <bool kAll>
 __global__ void WX_RAY_BOUNDS k_pixel(const __grid_constant__ Job job, uint32_t ntiles) {
+    // Let the next frame's launch start once every block of this one has begun.
+    asm volatile("griddepcontrol.launch_dependents;");
     const uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (tile >= ntiles) return;
     render_pixel<kAll>(job, tile, threadIdx.x & 31u);
@@ -186,10 +192,20 @@ int max_blocks_per_sm(int kernel, bool batched, int warps_per_block) {
 
 cudaError_t launch_pixel(const Job &job, const Tuning &t, cudaStream_t st) {
     const uint32_t wpb = (uint32_t)t.warps_per_block;
-    const unsigned blocks = (job.tiles + wpb - 1) / wpb;
-    if (all_modes(job.s)) k_pixel<true><<<blocks, 32 * wpb, 0, st>>>(job, job.tiles);
-    else k_pixel<false><<<blocks, 32 * wpb, 0, st>>>(job, job.tiles);
-    return cudaGetLastError();
+    // Programmatic dependent launch: back-to-back frames on one stream overlap
+    // the previous frame's last blocks with this frame's march (the kernel's
+    // stores wait for the previous kernel; see render_pixel).
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((job.tiles + wpb - 1) / wpb);
+    cfg.blockDim = dim3(32 * wpb);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (all_modes(job.s)) return cudaLaunchKernelEx(&cfg, k_pixel<true>, job, job.tiles);
+    return cudaLaunchKernelEx(&cfg, k_pixel<false>, job, job.tiles);
 }
 
 static int grid_blocks(const Tuning &t, bool batched, int num_sms, uint32_t total_tiles) {
