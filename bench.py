@@ -406,6 +406,8 @@ def main():
     ap.add_argument("--tile-width", type=int, default=None)
     ap.add_argument("--warps-per-block", type=int, default=None)
     ap.add_argument("--blocks-per-sm", type=int, default=None)
+    ap.add_argument("--tile-order", type=int, default=None, choices=[0, 1],
+                    help="0 tile rows top to bottom, 1 middle rows first")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args, args.workload)
@@ -437,7 +439,7 @@ def main():
     t_gen = time.perf_counter() - t0
     ctx = wx.Context(local)
     tune = {"kernel": 0 if args.kernel == "persistent" else 1}
-    for k in ("tile_width", "warps_per_block", "blocks_per_sm"):
+    for k in ("tile_width", "warps_per_block", "blocks_per_sm", "tile_order"):
         if getattr(args, k) is not None:
             tune[k] = getattr(args, k)
     ctx.set_tuning(**tune)
@@ -469,11 +471,13 @@ def main():
                 events[i][1].record(stream)
 
     tuned = None
-    if args.autotune and args.kernel == "persistent" and args.tile_width is None and args.warps_per_block is None:
+    if (args.autotune and args.kernel == "persistent" and args.tile_width is None and args.warps_per_block is None
+            and args.tile_order is None):
         t0 = time.perf_counter()
         tuned = ctx.autotune([(grid, st, W_, H_, o, None) for st, o in list(zip(states, outs))[:4]], reps=2)
         tuned["seconds"] = time.perf_counter() - t0
-        tuned["table"] = [[c["kernel"], c["tile_width"], c["warps_per_block"], c["blocks_per_sm"], round(ms, 4)]
+        tuned["table"] = [[c["kernel"], c["tile_width"], c["warps_per_block"], c["blocks_per_sm"], c["tile_order"],
+                           round(ms, 4)]
                           for c, ms in tuned["table"]]
         log(f"[bench] autotune -> {tuned['best']} in {tuned['seconds']:.1f}s")
     for _ in range(args.warmup):
@@ -654,7 +658,7 @@ def main():
                        "grid_build_s": {"host_sdf": round(t_build, 3), "gpu_sdf": round(t_build_gpu, 3)},
                        "render_mode": frames[0].mode, "l2": "flushed between steps (512 MB write)",
                        "parallelism": f"replicas x{world}", "tuning": ctx.tuning,
-                       "autotune": tuned and {"table [kernel, tile_w, warps/block, blocks/SM (0 = all that fit), ms for 4 frames]":
+                       "autotune": tuned and {"table [kernel, tile_w, warps/block, blocks/SM (0 = all that fit), tile order (1 = middle rows first), ms for 4 frames]":
                                               tuned["table"],
                                               "seconds": tuned["seconds"]}},
             "frame_latency_ms": {"p50": p50, "p99": p99},

@@ -119,6 +119,11 @@ typedef struct wx_tuning {
     int32_t blocks_per_sm;   /* persistent kernel: 0 = as many as fit */
     int32_t tile_width;      /* pixel tile of one warp: 4, 8 (default: the reference's 8x4
                                 workgroup), 16 or 32 wide, 32/tile_width high */
+    int32_t tile_order;      /* order in which tile rows are handed out: 0 top to bottom;
+                                1 (default) the middle row first, then alternately the rows
+                                above and below it, so that the costly centre of a centred
+                                view starts first and a frame's last tiles are its cheap
+                                edges. The pixels written are the same either way. */
 } wx_tuning;
 
 /* One frame of a batched launch: a camera uniform over one resident grid. */
@@ -189,10 +194,10 @@ int wx_ctx_get_tuning(const wx_ctx *ctx, wx_tuning *tuning);
 /* Autotuner: renders `frames` (device outputs, as for wx_render_batch) once per
  * frame with each candidate tuning, reps times after one warm-up pass, timing
  * with CUDA events, and installs the fastest on the context. candidates NULL
- * (ncand ignored) uses the built-in set: both kernels x tile widths {4, 8, 16}
- * x {2, 4, 8} warps per block, plus the persistent kernel at 4 blocks of 4
- * warps per SM (tile widths 4, 8). times_ms (ncand or 20 entries, may be NULL)
- * receives each candidate's mean time for all frames. */
+ * (ncand ignored) uses the built-in set: for tile orders 1 then 0, both kernels
+ * x tile widths {4, 8, 16} x {2, 4, 8} warps per block, plus the persistent
+ * kernel at 4 blocks of 4 warps per SM (tile widths 4, 8). times_ms (ncand or
+ * 40 entries, may be NULL) receives each candidate's mean time for all frames. */
 int wx_autotune(wx_ctx *ctx, const wx_frame *frames, uint32_t n, const wx_tuning *candidates, uint32_t ncand,
                 uint32_t reps, wx_tuning *best, double *times_ms);
 

@@ -55,7 +55,8 @@ def test_tuning_rejects_out_of_range_values(cuda_ctx, sphere):
     _, view, grid = sphere
     before = cuda_ctx.tuning
     for bad in [dict(kernel=3), dict(kernel=-1), dict(tile_width=12), dict(warps_per_block=0),
-                dict(warps_per_block=9), dict(blocks_per_sm=-1), dict(blocks_per_sm=65)]:
+                dict(warps_per_block=9), dict(blocks_per_sm=-1), dict(blocks_per_sm=65), dict(tile_order=2),
+                dict(tile_order=-1)]:
         with pytest.raises(wx.WxError, match="range"):
             cuda_ctx.set_tuning(**dict(before, **bad))
         assert cuda_ctx.tuning == before

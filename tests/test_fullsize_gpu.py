@@ -67,8 +67,8 @@ def test_spheres_batched_equals_plain_and_repeatable(cuda_ctx, spheres):
 
 @pytest.mark.parametrize("mode", [3, 0])
 def test_spheres_all_kernels_agree(cuda_ctx, spheres, mode):
-    """Whole 1080p frames: the per-tile kernel and other tile shapes write the same RGBA8 and
-    hit records as the tile-queue kernel, bit for bit."""
+    """Whole 1080p frames: the per-tile kernel, other tile shapes and both tile-row orders write
+    the same RGBA8 and hit records as the tile-queue kernel, bit for bit."""
     _, _, grid = spheres
     before = cuda_ctx.tuning
     try:
@@ -76,8 +76,8 @@ def test_spheres_all_kernels_agree(cuda_ctx, spheres, mode):
             st = f.state()
             st.render_mode[0] = mode
             outs = []
-            for k, tw in ((0, 8), (1, 4), (0, 16), (1, 32)):
-                cuda_ctx.set_tuning(kernel=k, tile_width=tw)
+            for k, tw, order in ((0, 8, 1), (1, 4, 1), (0, 16, 0), (1, 32, 1), (1, 4, 0), (0, 4, 0)):
+                cuda_ctx.set_tuning(kernel=k, tile_width=tw, tile_order=order)
                 outs.append(gpu_render(cuda_ctx, grid, st, f.width, f.height))
             for rg, hg in outs[1:]:
                 np.testing.assert_array_equal(rg, outs[0][0])

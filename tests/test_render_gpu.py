@@ -8,14 +8,16 @@ from parity import compare, dispatch_mask, gpu_render, oracle_render
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(params=["persistent", "pixel", "pixel-16x2", "persistent-4x8", "persistent-4blocks"], autouse=True)
+@pytest.fixture(params=["persistent", "pixel", "pixel-16x2", "persistent-4x8", "persistent-4blocks", "pixel-rows"],
+                autouse=True)
 def kernel(request, cuda_ctx):
-    """Run every parity test on both kernels, on non-default pixel tile shapes and at reduced occupancy."""
+    """Run every parity test on both kernels, on non-default pixel tile shapes, at reduced occupancy
+    and with tile rows handed out top to bottom."""
     before = cuda_ctx.tuning
     tw = {"pixel-16x2": 16, "persistent-4x8": 4}.get(request.param, 8)
     bps = 4 if request.param == "persistent-4blocks" else 0
     cuda_ctx.set_tuning(kernel=0 if request.param.startswith("persistent") else 1, tile_width=tw,
-                        blocks_per_sm=bps, warps_per_block=4)
+                        blocks_per_sm=bps, warps_per_block=4, tile_order=0 if request.param == "pixel-rows" else 1)
     yield request.param
     cuda_ctx.set_tuning(**before)
 

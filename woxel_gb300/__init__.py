@@ -335,9 +335,11 @@ class Context:
         install the fastest. Returns {"best": tuning, "table": [(tuning, ms), ...]}."""
         arr = self._frames(frames)
         if candidates is None:
-            cands = [dict(kernel=k, warps_per_block=w, blocks_per_sm=0, tile_width=t)
-                     for k in (0, 1) for t in (4, 8, 16) for w in (2, 4, 8)]
-            cands += [dict(kernel=0, warps_per_block=4, blocks_per_sm=4, tile_width=t) for t in (4, 8)]
+            cands = []
+            for o in (1, 0):  # the built-in set of wx_autotune, in its order
+                cands += [dict(kernel=k, warps_per_block=w, blocks_per_sm=0, tile_width=t, tile_order=o)
+                          for k in (0, 1) for t in (4, 8, 16) for w in (2, 4, 8)]
+                cands += [dict(kernel=0, warps_per_block=4, blocks_per_sm=4, tile_width=t, tile_order=o) for t in (4, 8)]
         else:
             cands = [dict(self.tuning, **c) for c in candidates]
         carr = (wx_tuning * len(cands))(*[wx_tuning(**c) for c in cands])

@@ -37,7 +37,7 @@ class wx_grid_info(C.Structure):
 
 class wx_tuning(C.Structure):
     _fields_ = [("kernel", C.c_int32), ("warps_per_block", C.c_int32), ("blocks_per_sm", C.c_int32),
-                ("tile_width", C.c_int32)]
+                ("tile_width", C.c_int32), ("tile_order", C.c_int32)]
 
 
 class wx_frame(C.Structure):

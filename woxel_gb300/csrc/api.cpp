@@ -295,14 +295,15 @@ int upload_pools(wx_ctx *ctx, const std::vector<int4> &o5, const uint32_t *s5, c
 // Tiles of tile_w x (32 / tile_w) pixels over the dispatched region
 // 8*floor(w/8) x 4*floor(h/4) (wgpu_context.rs:281).
 wxk::Job make_job(const wx_grid *grid, const wx_state_uniform &s, uint32_t width, uint32_t height, uint32_t *rgba,
-                  wx_hit *hits, uint32_t tile_begin, int tile_w) {
+                  wx_hit *hits, uint32_t tile_begin, const wxk::Tuning &t) {
     wxk::Job j;
     memset(&j, 0, sizeof j);
     j.g = grid->g;
     j.width = width;
     j.height = height;
-    j.tile_w = (uint32_t)tile_w;
-    j.tile_h = 32u / j.tile_w;
+    j.tile_w = (uint16_t)t.tile_w;
+    j.order = (uint32_t)t.order;
+    j.tile_h = (uint16_t)(32u / j.tile_w);
     const uint32_t wd = width & ~7u, hd = height & ~3u;
     j.tiles_x = (wd + j.tile_w - 1) / j.tile_w;
     j.tiles = j.tiles_x * ((hd + j.tile_h - 1) / j.tile_h);
@@ -394,12 +395,13 @@ int wx_ctx_set_tuning(wx_ctx *ctx, const wx_tuning *t) {
     if (!ctx || !t) return fail(ctx, WX_ERR_INVALID, "wx_ctx_set_tuning: null argument");
     const bool tw_ok = t->tile_width == 4 || t->tile_width == 8 || t->tile_width == 16 || t->tile_width == 32;
     if (t->kernel < 0 || t->kernel > 1 || t->warps_per_block < 1 || t->warps_per_block > 8 || t->blocks_per_sm < 0 ||
-        t->blocks_per_sm > 64 || !tw_ok)
+        t->blocks_per_sm > 64 || !tw_ok || t->tile_order < 0 || t->tile_order > 1)
         return fail(ctx, WX_ERR_INVALID, "wx_ctx_set_tuning: value out of range");
     ctx->tuning.kernel = t->kernel;
     ctx->tuning.warps_per_block = t->warps_per_block;
     ctx->tuning.blocks_per_sm = t->blocks_per_sm;
     ctx->tuning.tile_w = t->tile_width;
+    ctx->tuning.order = t->tile_order;
     return WX_OK;
 }
 
@@ -409,6 +411,7 @@ int wx_ctx_get_tuning(const wx_ctx *ctx, wx_tuning *t) {
     t->warps_per_block = ctx->tuning.warps_per_block;
     t->blocks_per_sm = ctx->tuning.blocks_per_sm;
     t->tile_width = ctx->tuning.tile_w;
+    t->tile_order = ctx->tuning.order;
     return WX_OK;
 }
 
@@ -420,11 +423,13 @@ int wx_autotune(wx_ctx *ctx, const wx_frame *frames, uint32_t n, const wx_tuning
     if (candidates) {
         cand.assign(candidates, candidates + ncand);
     } else {
-        for (int kernel : {0, 1})
-            for (int tw : {4, 8, 16})
-                for (int wpb : {2, 4, 8}) cand.push_back(wx_tuning{kernel, wpb, 0, tw});
-        // Occupancy of the persistent kernel: fewer resident warps than fit (16 per SM).
-        for (int tw : {4, 8}) cand.push_back(wx_tuning{0, 4, 4, tw});
+        for (int order : {1, 0}) {
+            for (int kernel : {0, 1})
+                for (int tw : {4, 8, 16})
+                    for (int wpb : {2, 4, 8}) cand.push_back(wx_tuning{kernel, wpb, 0, tw, order});
+            // Occupancy of the persistent kernel: fewer resident warps than fit (16 per SM).
+            for (int tw : {4, 8}) cand.push_back(wx_tuning{0, 4, 4, tw, order});
+        }
     }
     if (cand.empty()) return fail(ctx, WX_ERR_INVALID, "wx_autotune: no candidates");
     for (uint32_t i = 0; i < n; i++)
@@ -864,7 +869,7 @@ int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, u
         if (!dev_rgba) out_rgba = reinterpret_cast<uint32_t *>(b);
         if (hits && !dev_hits) out_hits = reinterpret_cast<wx_hit *>(b + ((npix * 4 + 255) & ~(size_t)255));
     }
-    const wxk::Job job = make_job(grid, *state, width, height, out_rgba, out_hits, 0, ctx->tuning.tile_w);
+    const wxk::Job job = make_job(grid, *state, width, height, out_rgba, out_hits, 0, ctx->tuning);
     if (ctx->tuning.kernel == 1) WX_CUDA(ctx, wxk::launch_pixel(job, ctx->tuning, st));
     else WX_CUDA(ctx, wxk::launch_persistent(job, ctx->take_counter(), ctx->tuning, ctx->num_sms, st));
     // Copy back only the dispatched region; the rest of a host buffer is untouched.
@@ -893,7 +898,7 @@ static int build_jobs(wx_ctx *ctx, const wx_frame *frames, uint32_t n, std::vect
             return fail(ctx, WX_ERR_INVALID, "wx_frame: batched outputs must be device memory");
         if ((uint64_t)f.width * f.height >= (1ull << 32)) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_frame: too large");
         const wxk::Job j = make_job(f.grid, f.state, f.width, f.height, reinterpret_cast<uint32_t *>(f.rgba8), f.hits,
-                                    (uint32_t)tiles, ctx->tuning.tile_w);
+                                    (uint32_t)tiles, ctx->tuning);
         if (j.tiles == 0) continue;
         jobs.push_back(j);
         tiles += j.tiles;

@@ -31,8 +31,15 @@ using wxk::Job;
 // chain and the zero-crossing search would otherwise cost the march registers.
 template <bool kAll>
 __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t lane) {
+    // Tile row: with order 1, the i-th row handed out is the middle row, then
+    // alternately the rows above and below it (a permutation of the rows).
+    uint32_t row = tl / J.tiles_x;
+    if (J.order) {
+        const uint32_t mid = (J.tiles / J.tiles_x) >> 1;
+        row = (row & 1u) ? mid - ((row + 1u) >> 1) : mid + (row >> 1);
+    }
     const uint32_t gx = (tl % J.tiles_x) * J.tile_w + lane % J.tile_w;
-    const uint32_t gy = (tl / J.tiles_x) * J.tile_h + lane / J.tile_w;
+    const uint32_t gy = row * J.tile_h + lane / J.tile_w;
     // The warp's lanes leave each march at different iterations. Without the
     // explicit reconvergence points below they go on in small groups, each
     // running the shading once and starting its own shadow march.
@@ -345,8 +352,9 @@ int noalloc_render(int device, const wx_frame *frames, uint32_t n, cudaStream_t 
             return noalloc_fail(WX_ERR_UNSUPPORTED, "wx_render_batch_noalloc: frame too large");
         j.width = f.width;
         j.height = f.height;
-        j.tile_w = (uint32_t)tuning.tile_w;
-        j.tile_h = 32u / j.tile_w;
+        j.tile_w = (uint16_t)tuning.tile_w;
+        j.tile_h = (uint16_t)(32 / tuning.tile_w);
+        j.order = (uint32_t)tuning.order;
         j.tiles_x = ((f.width & ~7u) + j.tile_w - 1) / j.tile_w;
         j.tiles = j.tiles_x * (((f.height & ~3u) + j.tile_h - 1) / j.tile_h);
         j.tile_begin = (uint32_t)tiles;

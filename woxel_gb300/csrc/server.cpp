@@ -215,6 +215,7 @@ struct wx_server {
             j.height = q->r.height;
             j.tile_w = kTileW;
             j.tile_h = kTileH;
+            j.order = (uint32_t)wxk::Tuning().order;
             j.tiles_x = (q->r.width & ~7u) / kTileW;
             j.tiles = q->tiles;
             j.tile_begin = tiles;

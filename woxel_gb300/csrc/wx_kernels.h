@@ -25,7 +25,8 @@ struct DevGrid {
 struct Job {
     DevGrid g;
     uint32_t width, height;
-    uint32_t tile_w, tile_h;       // pixel tile of one warp (tile_w * tile_h = 32)
+    uint16_t tile_w, tile_h;       // pixel tile of one warp (tile_w * tile_h = 32)
+    uint32_t order;                // tile rows: 0 top to bottom, 1 middle row first, then outwards
     uint32_t tiles_x, tiles;       // tiles per row / per frame over the dispatched region
     uint32_t tile_begin;           // first global (queue) tile id of this job
     uint32_t tile_off;             // first frame tile of this job (a job may cover part of a frame)
@@ -39,6 +40,7 @@ struct Tuning {
     int warps_per_block = 4;   // 1..16
     int blocks_per_sm = 0;     // 0 = as many as fit
     int tile_w = 8;            // 4, 8, 16 or 32 pixels wide (x 32/tile_w high)
+    int order = 1;             // Job::order
 };
 
 cudaError_t init_device_tables();
