@@ -135,7 +135,8 @@ __device__ __forceinline__ uint32_t ray_mask(const Ray &r) {
 __device__ __forceinline__ bool ray_needs_careful_step(F3 src, F3 dir) {
     const bool neg0 = (__float_as_uint(src.x) == 0x80000000u) | (__float_as_uint(src.y) == 0x80000000u) |
                       (__float_as_uint(src.z) == 0x80000000u);
-    return neg0 || !(fminf(fminf(fabsf(dir.x), fabsf(dir.y)), fabsf(dir.z)) >= 0x1p-126f);
+    // Each comparison is false for NaN (fminf would drop a NaN component).
+    return neg0 || !(fabsf(dir.x) >= 0x1p-126f && fabsf(dir.y) >= 0x1p-126f && fabsf(dir.z) >= 0x1p-126f);
 }
 
 // Exact distance of a leaf voxel whose byte is 255 (distance >= 255): binary
