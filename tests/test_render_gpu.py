@@ -192,6 +192,27 @@ def test_edge_cameras(cuda_ctx, sphere64):
             compare(rg, hg, ro, ho, label=f"eye{eye}/mode{mode}")
 
 
+def test_nodes_beyond_the_bound(cuda_ctx):
+    """N5 nodes outside [-4096, 4096)^3: the bounds test then runs on every step (it is skipped
+    inside N5s only when all N5s lie in that box). Rays cross voxels on both sides of +-4096."""
+    rng = np.random.default_rng(17)
+    ijk = np.concatenate([rng.integers(4080, 4112, size=(3000, 3)), rng.integers(-4112, -4080, size=(3000, 3)),
+                          rng.integers(5000, 5100, size=(500, 3))]).astype(np.int32)
+    topo = wx.Topology.from_voxels(ijk)
+    view = topo.view()
+    grid = cuda_ctx.build_grid(topo)
+    for eye, target in [((4000.0, 4000.0, 3950.0), (4100.0, 4100.0, 4100.0)),
+                        ((4200.0, 4150.0, 4300.0), (4096.0, 4096.0, 4096.0)),
+                        ((-4000.0, -4010.0, -3900.0), (-4100.0, -4100.0, -4100.0)),
+                        ((4500.0, 4500.0, 4500.0), (5050.0, 5050.0, 5050.0))]:
+        for mode in (0, 3):
+            st = wx.state_build(eye=eye, target=target, aspect=1.0, fovy=70.0, width=64.0, mode=mode)
+            rg, hg = gpu_render(cuda_ctx, grid, st, 64, 64)
+            ro, ho = oracle_render(view, st, 64, 64)
+            compare(rg, hg, ro, ho, label=f"beyond/{eye}/mode{mode}")
+    grid.release()
+
+
 def test_zero_direction_components(cuda_ctx, sphere64):
     """Rays with an exactly-zero direction component (1/dir = inf) take the NaN-aware step."""
     _, view, grid = sphere64

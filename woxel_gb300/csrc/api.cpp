@@ -226,6 +226,10 @@ int alloc_grid(wx_ctx *ctx, const std::vector<int4> &o5, uint64_t n5, uint64_t n
     gr->g.ovf = reinterpret_cast<const uint2 *>(b + b_o5 + b5 + b4 + b3);
     gr->g.n5 = (uint32_t)n5;
     gr->g.n_ovf = (uint32_t)n_ovf;
+    gr->g.inside = 1u;
+    for (uint64_t i = 0; i < n5; i++)
+        for (int c : {o5[i].x, o5[i].y, o5[i].z})
+            if (c != -4096 && c != 0) gr->g.inside = 0u;
     gr->info.n5 = n5;
     gr->info.n4 = n4;
     gr->info.n3 = n3;

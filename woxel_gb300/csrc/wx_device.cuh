@@ -243,7 +243,11 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     if (dist == 0u) return 0u;
     const float apx = fabsf(r.px), apy = fabsf(r.py), apz = fabsf(r.pz);
     // any(4096 < |p|); a NaN coordinate compares false, and fmaxf skips NaN.
-    if (4096.0f < fmaxf(fmaxf(apx, apy), apz)) return 1u;
+    // Not needed when this step found an N5 (r.np >= 1) of a grid whose N5s
+    // all lie in [-4096, 4096)^3: then floor(p) is in that box, so |p| <= 4096.
+    // (The fast step makes no NaN coordinate; an infinite one floors outside
+    // every N5, so its step has r.np == 0 and is tested.)
+    if ((kCareful || r.np == 0u || !g.inside) && 4096.0f < fmaxf(fmaxf(apx, apy), apz)) return 1u;
     // size = f32(dist) * scale[by num_parents] (:105-112); log2 scale by np = 12, 7, 3, 0.
     const float size = __uint2float_rn(dist) * __uint_as_float(sbits);
     bool fast;

@@ -19,6 +19,7 @@ struct DevGrid {
     const float *values;     // level-set value per leaf voxel (zero-crossing mode), or null
     uint32_t n5, n_ovf;
     float band;              // value of voxels outside leaves (+band; -band in active tiles)
+    uint32_t inside;         // every N5 lies in [-4096, 4096)^3 (origins -4096 or 0 on each axis)
 };
 
 // One frame of one grid: the unit the persistent kernels draw ray tiles from.
