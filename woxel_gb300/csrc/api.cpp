@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -92,6 +93,56 @@ int cuda_fail(wx_ctx *ctx, cudaError_t e, const char *what) {
         cudaError_t e_ = (call);                                 \
         if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
     } while (0)
+
+// Output byte ranges [lo, hi) (rgba8, hit records) of the last k_pixel launched
+// on each (device, stream). A k_pixel launch's predecessor on its stream is
+// either the k_pixel recorded here (the only kernel of this library that lets
+// its dependents start early) or work after which nothing overlaps; k_pixel
+// itself keeps frames older than the predecessor finished (kernels.cu). So a
+// frame whose outputs are disjoint from the record's need not wait before its
+// stores. A stream without a record counts as overlapping.
+struct PixelOutputs {
+    int device;
+    cudaStream_t stream;
+    uintptr_t lo[2], hi[2];
+};
+constexpr size_t kPixelStreams = 256;  // records kept, oldest dropped first
+std::mutex g_pixel_mu;
+std::vector<PixelOutputs> g_pixel_outputs;
+
+// Records cur as its stream's last k_pixel; true when disjoint from the previous record.
+bool pixel_outputs_disjoint(const PixelOutputs &cur) {
+    auto meet = [](uintptr_t a0, uintptr_t a1, uintptr_t b0, uintptr_t b1) {
+        return a0 < a1 && b0 < b1 && a0 < b1 && b0 < a1;
+    };
+    std::lock_guard<std::mutex> lock(g_pixel_mu);
+    auto &v = g_pixel_outputs;
+    bool disjoint = false;
+    size_t i = 0;
+    while (i < v.size() && !(v[i].device == cur.device && v[i].stream == cur.stream)) i++;
+    if (i < v.size()) {
+        disjoint = true;
+        for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 2; b++)
+                if (meet(cur.lo[a], cur.hi[a], v[i].lo[b], v[i].hi[b])) disjoint = false;
+        v.erase(v.begin() + (long)i);
+    } else if (v.size() >= kPixelStreams) {
+        v.erase(v.begin());
+    }
+    v.push_back(cur);
+    return disjoint;
+}
+
+// After a failed launch the stream's last kernel is unknown.
+void forget_pixel_outputs(int device, cudaStream_t st) {
+    std::lock_guard<std::mutex> lock(g_pixel_mu);
+    auto &v = g_pixel_outputs;
+    for (size_t i = 0; i < v.size(); i++)
+        if (v[i].device == device && v[i].stream == st) {
+            v.erase(v.begin() + (long)i);
+            return;
+        }
+}
 
 bool device_accessible(const void *p) {
     cudaPointerAttributes a;
@@ -874,7 +925,21 @@ int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, u
         if (hits && !dev_hits) out_hits = reinterpret_cast<wx_hit *>(b + ((npix * 4 + 255) & ~(size_t)255));
     }
     const wxk::Job job = make_job(grid, *state, width, height, out_rgba, out_hits, 0, ctx->tuning);
-    if (ctx->tuning.kernel == 1) WX_CUDA(ctx, wxk::launch_pixel(job, ctx->tuning, st));
+    if (ctx->tuning.kernel == 1) {
+        PixelOutputs cur{ctx->device, st, {0, 0}, {0, 0}};
+        cur.lo[0] = reinterpret_cast<uintptr_t>(out_rgba);
+        cur.hi[0] = cur.lo[0] + npix * 4;
+        if (hits) {
+            cur.lo[1] = reinterpret_cast<uintptr_t>(out_hits);
+            cur.hi[1] = cur.lo[1] + npix * sizeof(wx_hit);
+        }
+        const bool disjoint = pixel_outputs_disjoint(cur);
+        const cudaError_t e = wxk::launch_pixel(job, ctx->tuning, disjoint, st);
+        if (e != cudaSuccess) {
+            forget_pixel_outputs(ctx->device, st);
+            return cuda_fail(ctx, e, "wxk::launch_pixel");
+        }
+    }
     else WX_CUDA(ctx, wxk::launch_persistent(job, ctx->take_counter(), ctx->tuning, ctx->num_sms, st));
     // Copy back only the dispatched region; the rest of a host buffer is untouched.
     if (!dev_rgba)

@@ -30,7 +30,7 @@ using wxk::Job;
 // host sends frames of modes 4 and 5 to the kAll = true kernels): the glossy
 // chain and the zero-crossing search would otherwise cost the march registers.
 template <bool kAll>
-__device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t lane) {
+__device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t lane, bool wait_prev) {
     // Tile row: with order 1, the i-th row handed out is the middle row, then
     // alternately the rows above and below it (a permutation of the rows).
     uint32_t row = tl / J.tiles_x;
@@ -87,10 +87,11 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
     }
     __syncwarp(act);
     const uint32_t pix = gy * J.width + gx;
-    // A programmatically dependent launch (launch_pixel) may run its march while
-    // the previous kernel of the stream finishes; its stores wait for that
-    // kernel to complete, so frames never overlap in memory. A no-op otherwise.
-    asm volatile("griddepcontrol.wait;" ::: "memory");
+    // A programmatically dependent launch (k_pixel) may run its march while the
+    // previous kernel of the stream finishes; unless that kernel's outputs are
+    // disjoint from this frame's, the stores wait for it to complete. A no-op
+    // in a launch that is not programmatically dependent.
+    if (wait_prev) asm volatile("griddepcontrol.wait;" ::: "memory");
     J.rgba[pix] = pack_rgba(c);
     if (J.hits)
         store_hit(J.hits + pix, hit.p, dot3(hit.p - eye, dir), hit.node,
@@ -104,13 +105,22 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
 // spills outside the march loop; 40 registers spill too much.
 #define WX_RAY_BOUNDS __launch_bounds__(256, 5)
 
+//
+// Frames on one stream overlap in time: the next k_pixel starts once every block
+// of this one has signalled launch_dependents. Block 0 signals only after the
+// previous kernel has completed, so (1) a frame completes after its predecessor,
+// and (2) a frame starts only after the frame two back has completed: while it
+// runs, at most the frame just before it is still writing. disjoint (set by the
+// host when this frame's outputs do not overlap that frame's) lets every block
+// write without waiting and retire as soon as its tiles are done, so the
+// previous frame's last blocks do not hold finished blocks on the SMs.
 template <bool kAll>
-__global__ void WX_RAY_BOUNDS k_pixel(const __grid_constant__ Job job, uint32_t ntiles) {
-    // Let the next frame's launch start once every block of this one has begun.
+__global__ void WX_RAY_BOUNDS k_pixel(const __grid_constant__ Job job, uint32_t ntiles, uint32_t disjoint) {
+    if (blockIdx.x == 0) asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;");
     const uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (tile >= ntiles) return;
-    render_pixel<kAll>(job, tile, threadIdx.x & 31u);
+    render_pixel<kAll>(job, tile, threadIdx.x & 31u, disjoint == 0u);
 }
 
 // First job whose tile range contains tile t (jobs sorted by tile_begin, no empty jobs).
@@ -141,9 +151,9 @@ __global__ void WX_RAY_BOUNDS k_persistent(const Job *__restrict__ jobs, uint32_
         if (kBatched) {
             cur_job = find_job(jobs, njobs, t, cur_job);
             const Job &J = jobs[cur_job];
-            render_pixel<kAll>(J, t - J.tile_begin + J.tile_off, lane);
+            render_pixel<kAll>(J, t - J.tile_begin + J.tile_off, lane, true);
         } else {
-            render_pixel<kAll>(job0, t, lane);
+            render_pixel<kAll>(job0, t, lane, true);
         }
     }
 }
@@ -197,7 +207,7 @@ int max_blocks_per_sm(int kernel, bool batched, int warps_per_block) {
     return batched ? blocks_for(k_persistent<true, false>, threads) : blocks_for(k_persistent<false, false>, threads);
 }
 
-cudaError_t launch_pixel(const Job &job, const Tuning &t, cudaStream_t st) {
+cudaError_t launch_pixel(const Job &job, const Tuning &t, bool disjoint, cudaStream_t st) {
     const uint32_t wpb = (uint32_t)t.warps_per_block;
     // Programmatic dependent launch: back-to-back frames on one stream overlap
     // the previous frame's last blocks with this frame's march (the kernel's
@@ -211,8 +221,9 @@ cudaError_t launch_pixel(const Job &job, const Tuning &t, cudaStream_t st) {
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (all_modes(job.s)) return cudaLaunchKernelEx(&cfg, k_pixel<true>, job, job.tiles);
-    return cudaLaunchKernelEx(&cfg, k_pixel<false>, job, job.tiles);
+    const uint32_t dj = disjoint ? 1u : 0u;
+    if (all_modes(job.s)) return cudaLaunchKernelEx(&cfg, k_pixel<true>, job, job.tiles, dj);
+    return cudaLaunchKernelEx(&cfg, k_pixel<false>, job, job.tiles, dj);
 }
 
 static int grid_blocks(const Tuning &t, bool batched, int num_sms, uint32_t total_tiles) {

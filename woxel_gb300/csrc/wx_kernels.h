@@ -46,7 +46,9 @@ struct Tuning {
 
 cudaError_t init_device_tables();
 int max_blocks_per_sm(int kernel, bool batched, int warps_per_block);
-cudaError_t launch_pixel(const Job &job, const Tuning &t, cudaStream_t st);
+// disjoint: the job's outputs do not overlap those of the previous kernel on st,
+// a k_pixel launch (see k_pixel); false is always safe.
+cudaError_t launch_pixel(const Job &job, const Tuning &t, bool disjoint, cudaStream_t st);
 cudaError_t launch_persistent(const Job &job, uint32_t *ctr, const Tuning &t, int num_sms, cudaStream_t st);
 // all: some job renders mode 4 or 5 (the kernels compiled for every mode).
 cudaError_t launch_batched(const Job *jobs_dev, uint32_t njobs, uint32_t total_tiles, uint32_t *ctr,
