@@ -183,7 +183,15 @@ int wx_grid_read_pools(wx_ctx *ctx, const wx_grid *grid, uint32_t *slot5, uint32
  * cudaStream_t (NULL = legacy default stream). Outputs in device memory or in
  * page-locked host memory are written by the kernel (complete when the stream
  * is synchronised); pageable host outputs are staged on the device and copied
- * back (complete on return). */
+ * back (complete on return).
+ * With tuning kernel 1 the frame is a programmatic dependent launch: it may start
+ * while the previous kernel on the stream finishes. When that kernel is the
+ * previous frame of this library and the outputs of the two frames do not
+ * overlap, the new frame writes without waiting for it; otherwise its writes
+ * wait for that kernel to complete. Stream order holds either way for the work
+ * after the frame. A kernel of the caller's own that lets its dependents start
+ * early (programmatic dependent launch) and immediately precedes the frame must
+ * not access the frame's outputs. */
 int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, uint32_t width,
               uint32_t height, uint8_t *rgba8, wx_hit *hits, void *stream);
 
