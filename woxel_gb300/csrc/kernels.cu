@@ -1,8 +1,9 @@
 // kernels.cu — sm_103a kernels of the raycast pass.
 //
 // k_pixel       one thread per pixel, one warp per pixel tile (8x4 by default:
-//               the reference's workgroup, raycast.comp.wgsl:60), tiles in
-//               launch order.
+//               the reference's workgroup, raycast.comp.wgsl:60), one launch per
+//               frame; consecutive frames on a stream overlap (programmatic
+//               dependent launch).
 // k_persistent  persistent warps drawing tiles from a global queue (an atomic
 //               counter in device scratch memory); kBatched = many frames
 //               (jobs) of several grids in one launch.
@@ -98,14 +99,13 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
                   hit.state | (hit.np << 2) | (hit.mask << 4) | (hit.i << 8), shadow, reserved);
 }
 
-// One warp per tile, tiles in launch order.
 // Blocks of at most 256 threads, at least 5 resident: 48 registers a thread and
 // 40 resident warps per SM. Measured on GB300 (2000-sphere frames): 48
 // registers beat 64 (32 warps) by 2% and 80 (24 warps) by 17% despite a few
 // spills outside the march loop; 40 registers spill too much.
 #define WX_RAY_BOUNDS __launch_bounds__(256, 5)
 
-//
+// One warp per tile of one frame, tiles in block order (rows in the job's order).
 // Frames on one stream overlap in time: the next k_pixel starts once every block
 // of this one has signalled launch_dependents. Block 0 signals only after the
 // previous kernel has completed, so (1) a frame completes after its predecessor,
