@@ -402,7 +402,8 @@ def main():
     ap.add_argument("--serve-duration", type=float, default=5.0, help="seconds of arrivals per rate")
     ap.add_argument("--serve-slice", type=int, default=65536, help="tiles per launch")
     ap.add_argument("--serve-timeout", type=float, default=300.0)
-    ap.add_argument("--kernel", default="persistent", choices=["persistent", "pixel"])
+    ap.add_argument("--kernel", default=None, choices=["persistent", "pixel"],
+                    help="fix the kernel (default: the autotuner's choice)")
     ap.add_argument("--tile-width", type=int, default=None)
     ap.add_argument("--warps-per-block", type=int, default=None)
     ap.add_argument("--blocks-per-sm", type=int, default=None)
@@ -438,7 +439,7 @@ def main():
     topo = wl.grids[wl.frames[0].grid]()
     t_gen = time.perf_counter() - t0
     ctx = wx.Context(local)
-    tune = {"kernel": 0 if args.kernel == "persistent" else 1}
+    tune = {} if args.kernel is None else {"kernel": 0 if args.kernel == "persistent" else 1}
     for k in ("tile_width", "warps_per_block", "blocks_per_sm", "tile_order"):
         if getattr(args, k) is not None:
             tune[k] = getattr(args, k)
@@ -471,7 +472,7 @@ def main():
                 events[i][1].record(stream)
 
     tuned = None
-    if (args.autotune and args.kernel == "persistent" and args.tile_width is None and args.warps_per_block is None
+    if (args.autotune and args.kernel is None and args.tile_width is None and args.warps_per_block is None
             and args.tile_order is None):
         t0 = time.perf_counter()
         tuned = ctx.autotune([(grid, st, W_, H_, o, None) for st, o in list(zip(states, outs))[:4]], reps=2)

@@ -113,8 +113,9 @@ typedef struct wx_batch wx_batch;
 
 /* Launch shape of the raycast kernels (set per context; see wx_ctx_set_tuning). */
 typedef struct wx_tuning {
-    int32_t kernel;          /* 0: persistent warps drawing pixel tiles from a queue (default);
-                                1: one warp per tile, tiles in launch order */
+    int32_t kernel;          /* 1 (default): one warp per pixel tile, one launch per frame,
+                                consecutive frames overlapping (see wx_render);
+                                0: persistent warps drawing pixel tiles from a queue */
     int32_t warps_per_block; /* 1..8 (default 4) */
     int32_t blocks_per_sm;   /* persistent kernel: 0 = as many as fit */
     int32_t tile_width;      /* pixel tile of one warp: 4, 8 (default: the reference's 8x4

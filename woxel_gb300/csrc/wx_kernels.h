@@ -37,7 +37,7 @@ struct Job {
 };
 
 struct Tuning {
-    int kernel = 0;            // 0 persistent warps on a tile queue, 1 one warp per tile in launch order
+    int kernel = 1;            // 1 one warp per tile (k_pixel), 0 persistent warps on a tile queue
     int warps_per_block = 4;   // 1..16
     int blocks_per_sm = 0;     // 0 = as many as fit
     int tile_w = 8;            // 4, 8, 16 or 32 pixels wide (x 32/tile_w high)
