@@ -99,11 +99,15 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
                   hit.state | (hit.np << 2) | (hit.mask << 4) | (hit.i << 8), shadow, reserved);
 }
 
-// Blocks of at most 256 threads, at least 5 resident: 48 registers a thread and
-// 40 resident warps per SM. Measured on GB300 (2000-sphere frames): 48
-// registers beat 64 (32 warps) by 2% and 80 (24 warps) by 17% despite a few
-// spills outside the march loop; 40 registers spill too much.
+// Blocks of at most 256 threads. The persistent kernels: at least 5 resident,
+// 48 registers a thread and 40 resident warps per SM. k_pixel: at least 6, 40
+// registers and 48 warps. Measured on GB300 (16 frames of 2000 spheres at
+// 1080p): k_pixel 3.17 Grays/s at 40 registers against 3.03 at 48 (its finished
+// blocks retire while the previous frame ends, so more resident warps pay); the
+// persistent kernels lose 6-8% at 40 registers (spills in the march loop) and
+// beat 64 (32 warps) by 2% and 80 (24 warps) by 17% at 48.
 #define WX_RAY_BOUNDS __launch_bounds__(256, 5)
+#define WX_PIXEL_BOUNDS __launch_bounds__(256, 6)
 
 // One warp per tile of one frame, tiles in block order (rows in the job's order).
 // Frames on one stream overlap in time: the next k_pixel starts once every block
@@ -115,7 +119,7 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
 // write without waiting and retire as soon as its tiles are done, so the
 // previous frame's last blocks do not hold finished blocks on the SMs.
 template <bool kAll>
-__global__ void WX_RAY_BOUNDS k_pixel(const __grid_constant__ Job job, uint32_t ntiles, uint32_t disjoint) {
+__global__ void WX_PIXEL_BOUNDS k_pixel(const __grid_constant__ Job job, uint32_t ntiles, uint32_t disjoint) {
     if (blockIdx.x == 0) asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;");
     const uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);

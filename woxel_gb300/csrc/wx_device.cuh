@@ -93,15 +93,15 @@ __device__ __forceinline__ uint32_t unorm8(float x) {
 // pool indices of the cached N5/N4/N3 plus the voxel of the previous lookup:
 // that voxel lies inside every cached node (levels 1..np), so "pos is in the
 // cached node of side S" is ((x ^ lx) | (y ^ ly) | (z ^ lz)) & ~(S - 1) == 0.
-// Per-ray constants: idir = 1/dir and step01 = max(0, sign11(dir)) (:86-88).
-// The nudge 4e-4 * step of :122 is (step01 - 0.5) * RN(8e-4), exactly
-// +-RN(4e-4) because RN commutes with scaling by two.
+// Per-ray constant: idir = 1/dir. step01 = max(0, sign11(dir)) (:86-88) is
+// 0 where dir < 0 and 1 elsewhere (NaN included); it is derived from dir in each
+// step rather than kept (fewer live registers). The nudge 4e-4 * step of :122 is
+// (step01 - 0.5) * RN(8e-4), exactly +-RN(8e-4) / 2 because RN commutes with
+// scaling by two.
 struct Ray {
     float px, py, pz;
     float dx, dy, dz;
     float ix, iy, iz;
-    float ax, ay, az;  // step01
-    float nx, ny, nz;  // 4e-4 * step
     int lx, ly, lz;
     uint32_t np, i5, i4, i3;
     uint32_t i;
@@ -112,8 +112,6 @@ __device__ __forceinline__ void ray_init(Ray &r, F3 src, F3 dir) {
     r.px = src.x; r.py = src.y; r.pz = src.z;
     r.dx = dir.x; r.dy = dir.y; r.dz = dir.z;
     r.ix = __frcp_rn(dir.x); r.iy = __frcp_rn(dir.y); r.iz = __frcp_rn(dir.z);
-    r.ax = pmax(0.0f, sign11(dir.x)); r.ay = pmax(0.0f, sign11(dir.y)); r.az = pmax(0.0f, sign11(dir.z));
-    r.nx = (r.ax - 0.5f) * 8e-4f; r.ny = (r.ay - 0.5f) * 8e-4f; r.nz = (r.az - 0.5f) * 8e-4f;
     r.lx = r.ly = r.lz = 0;
     r.np = 0; r.i5 = r.i4 = r.i3 = 0;
     r.mx = r.my = r.mz = false;
@@ -253,6 +251,7 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     bool fast;
     const float ys = rcp_size(dist, rbits, &fast);
     // tMax = idir * (size * step01 - (p - size * floor(p / size)))  (:78-80, :114)
+    const float ax = r.dx < 0.0f ? 0.0f : 1.0f, ay = r.dy < 0.0f ? 0.0f : 1.0f, az = r.dz < 0.0f ? 0.0f : 1.0f;
     float tx, ty, tz;
     // The fast quotient needs every coordinate of magnitude >= 2^-64 (a zero
     // coordinate also takes the IEEE path here; both give the same floor).
@@ -264,13 +263,13 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
         const float fx = floorf(div_fast(r.px, size, ys));
         const float fy = floorf(div_fast(r.py, size, ys));
         const float fz = floorf(div_fast(r.pz, size, ys));
-        tx = r.ix * __fmaf_rn(size, r.ax, -__fmaf_rn(-size, fx, r.px));
-        ty = r.iy * __fmaf_rn(size, r.ay, -__fmaf_rn(-size, fy, r.py));
-        tz = r.iz * __fmaf_rn(size, r.az, -__fmaf_rn(-size, fz, r.pz));
+        tx = r.ix * __fmaf_rn(size, ax, -__fmaf_rn(-size, fx, r.px));
+        ty = r.iy * __fmaf_rn(size, ay, -__fmaf_rn(-size, fy, r.py));
+        tz = r.iz * __fmaf_rn(size, az, -__fmaf_rn(-size, fz, r.pz));
     } else {
-        tx = r.ix * (size * r.ax - (r.px - size * floorf(__fdiv_rn(r.px, size))));
-        ty = r.iy * (size * r.ay - (r.py - size * floorf(__fdiv_rn(r.py, size))));
-        tz = r.iz * (size * r.az - (r.pz - size * floorf(__fdiv_rn(r.pz, size))));
+        tx = r.ix * (size * ax - (r.px - size * floorf(__fdiv_rn(r.px, size))));
+        ty = r.iy * (size * ay - (r.py - size * floorf(__fdiv_rn(r.py, size))));
+        tz = r.iz * (size * az - (r.pz - size * floorf(__fdiv_rn(r.pz, size))));
     }
     float t;
     bool mx, my, mz;
@@ -296,14 +295,17 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     r.mz = mz;
     // p += (4e-4 * step) * f32(mask)  (:122); without a -0 coordinate the
     // unmasked axes are unchanged.
+    const float kNudge = 0.5f * 8e-4f;
+    const float nx = ax != 0.0f ? kNudge : -kNudge, ny = ay != 0.0f ? kNudge : -kNudge,
+                nz = az != 0.0f ? kNudge : -kNudge;
     if (kCareful) {
-        r.px = r.px + r.nx * (mx ? 1.0f : 0.0f);
-        r.py = r.py + r.ny * (my ? 1.0f : 0.0f);
-        r.pz = r.pz + r.nz * (mz ? 1.0f : 0.0f);
+        r.px = r.px + nx * (mx ? 1.0f : 0.0f);
+        r.py = r.py + ny * (my ? 1.0f : 0.0f);
+        r.pz = r.pz + nz * (mz ? 1.0f : 0.0f);
     } else {
-        r.px = mx ? r.px + r.nx : r.px;
-        r.py = my ? r.py + r.ny : r.py;
-        r.pz = mz ? r.pz + r.nz : r.pz;
+        r.px = mx ? r.px + nx : r.px;
+        r.py = my ? r.py + ny : r.py;
+        r.pz = mz ? r.pz + nz : r.pz;
     }
     r.i++;
     return 0xFFu;
