@@ -259,7 +259,8 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
         // Here both products are exact, so each subtraction of a product is
         // one FMA with the same rounding: size * step01 is 0 or size, and
         // size * floor(p / size) = dist * f * 2^sk with |dist * f| <=
-        // 4096 / 2^sk + dist < 2^24 (|p| <= 4096 past the bounds test).
+        // 4096 / 2^sk + dist < 2^24 (|p| <= 4096 past the bounds test or where
+        // it was skipped).
         const float fx = floorf(div_fast(r.px, size, ys));
         const float fy = floorf(div_fast(r.py, size, ys));
         const float fz = floorf(div_fast(r.pz, size, ys));
