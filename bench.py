@@ -246,7 +246,7 @@ def run_reference(args, wl_name):
 # GPU arm
 # --------------------------------------------------------------------------
 def measure_mixed(ctx, grids, dev, flush, steps, warmup):
-    """BASELINE config 4: 256 requests over the sphere and 2000-sphere grids with resolutions
+    """Mixed requests: 256 requests over the sphere and 2000-sphere grids with resolutions
     uniform over {256^2, 640x480, 1280x720, 1920x1080, 3840x2160}. Plain = one wx_render
     launch per request on one stream; batched = one persistent launch over all requests,
     replayed from a CUDA graph (wx_batch_launch). Both device-timed with CUDA events."""
@@ -307,8 +307,9 @@ def measure_mixed(ctx, grids, dev, flush, steps, warmup):
 
 
 def run_serve(args):
-    """BASELINE config 5: open-loop Poisson arrivals over 8 resident grids (4 sphere-generator
-    grids with distinct seeds, 4 2000-sphere grids with seeds 2..5), resolution mix of config 4,
+    """Serving: open-loop Poisson arrivals over 8 resident grids (4 sphere-generator
+    grids with distinct seeds, 4 2000-sphere grids with seeds 2..5), the resolution mix of the
+    mixed requests,
     HBM budget 150 GB. Each rate is replayed on the continuous-batching server and on the FIFO
     single-request server; reports p50/p99 request latency and served Grays/s."""
     import torch
@@ -397,7 +398,7 @@ def main():
     ap.add_argument("--no-surface", action="store_true", help="skip the zero-crossing mode (render mode 5) figure")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default launch shape instead of autotuning on 4 frames")
-    ap.add_argument("--serve", action="store_true", help="run the serving sweep (config 5) instead")
+    ap.add_argument("--serve", action="store_true", help="run the serving sweep (Poisson arrivals over 8 grids) instead")
     ap.add_argument("--serve-rates", default="100,200,500,1000,2000,5000")
     ap.add_argument("--serve-duration", type=float, default=5.0, help="seconds of arrivals per rate")
     ap.add_argument("--serve-slice", type=int, default=65536, help="tiles per launch")
@@ -611,7 +612,7 @@ def main():
                    "note": "zero-crossing hit mode (extension, no reference counterpart): primary HDDA, then "
                            "trilinear level-set search and secant; not part of value"}
 
-    # BASELINE config 4: batched vs plain on the mixed-resolution load (needs the 2000-sphere grid)
+    # Batched vs plain on the mixed-resolution load (needs the 2000-sphere grid)
     batched = None
     if not args.no_batched and args.workload == "spheres":
         sphere_grid = ctx.build_grid(W.sphere_topology())
