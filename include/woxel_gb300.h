@@ -33,7 +33,7 @@ extern "C" {
 #define WX_ERR_INVALID 1      /* bad argument or malformed grid */
 #define WX_ERR_CUDA 2         /* a CUDA runtime call failed */
 #define WX_ERR_OOM 3          /* device or host allocation failed */
-#define WX_ERR_UNSUPPORTED 4  /* valid input outside what this build handles */
+#define WX_ERR_UNSUPPORTED 4  /* valid input outside what this library handles */
 #define WX_ERR_BUDGET 5       /* request does not fit the memory budget */
 #define WX_ERR_TIMEOUT 6      /* a bounded wait expired */
 #define WX_ERR_CANCELLED 7    /* work was cancelled */

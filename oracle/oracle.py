@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
-CPU-baseline / reference arms of bench.py as the checker. The product never
+CPU-baseline / reference arms of bench.py, to check and to time. The product never
 imports this module.
 """
 from __future__ import annotations

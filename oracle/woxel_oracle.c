@@ -1,7 +1,7 @@
 /*
  * woxel_oracle.c — CPU oracle for woxel's primary-ray pass (see woxel_oracle.h).
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path, never part of it.
+ * TEST INFRASTRUCTURE ONLY: what the CUDA path is checked against, never part of it.
  * Build with -O2 -ffp-contract=off (no FMA contraction, IEEE '/' and sqrt).
  *
  * Every function cites the reference file:line it restates. The structure of

@@ -1,8 +1,8 @@
 /*
  * woxel_oracle.h — CPU oracle for woxel's primary-ray pass.
  *
- * TEST INFRASTRUCTURE ONLY. This is the checker that the CUDA path is compared
- * against; nothing in the product links, loads or calls it. Only tests/,
+ * TEST INFRASTRUCTURE ONLY. The CUDA path is compared against this oracle;
+ * nothing in the product links, loads or calls it. Only tests/,
  * __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm use it.
  *
  * It restates, in plain C with IEEE binary32 arithmetic and no contraction
