@@ -939,8 +939,9 @@ int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, u
             forget_pixel_outputs(ctx->device, st);
             return cuda_fail(ctx, e, "wxk::launch_pixel");
         }
+    } else {
+        WX_CUDA(ctx, wxk::launch_persistent(job, ctx->take_counter(), ctx->tuning, ctx->num_sms, st));
     }
-    else WX_CUDA(ctx, wxk::launch_persistent(job, ctx->take_counter(), ctx->tuning, ctx->num_sms, st));
     // Copy back only the dispatched region; the rest of a host buffer is untouched.
     if (!dev_rgba)
         WX_CUDA(ctx, cudaMemcpy2DAsync(rgba8, (size_t)width * 4, out_rgba, (size_t)width * 4, (size_t)tiles_x * 32,
