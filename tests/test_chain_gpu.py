@@ -81,6 +81,24 @@ def test_partly_overlapping_outputs(cuda_ctx, scene):
     np.testing.assert_array_equal(buf.cpu().numpy(), want)
 
 
+def test_colour_of_one_frame_over_hit_records_of_the_last(cuda_ctx, scene):
+    """Frames alternate between two layouts in one buffer, so that each frame's RGBA8
+    and hit records land on the previous frame's hit records. Expected: the writes applied
+    in order."""
+    grid, states, refs = scene
+    n4, n32 = NPIX * 4, NPIX * 32
+    buf = torch.zeros(n4 + n4 + n32, dtype=torch.uint8, device="cuda")
+    want = np.zeros(n4 + n4 + n32, np.uint8)
+    layouts = [(0, n4), (n4, n4 + n4)]  # (rgba offset, hits offset)
+    for k, st in enumerate(states):
+        ro, ho = layouts[k % 2]
+        cuda_ctx.render(grid, st, 1920, 1080, buf[ro:ro + n4], buf[ho:ho + n32])
+        want[ro:ro + n4] = refs[k][0]
+        want[ho:ho + n32] = refs[k][1]
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(buf.cpu().numpy(), want)
+
+
 def test_two_contexts_on_one_stream(cuda_ctx, scene):
     grid, states, refs = scene
     other = wx.Context(0)
