@@ -139,7 +139,9 @@ __device__ __forceinline__ bool ray_needs_careful_step(F3 src, F3 dir) {
 
 // Exact distance of a leaf voxel whose byte is 255 (distance >= 255): binary
 // search of the grid's sorted overflow table, which holds every such voxel.
-__device__ __noinline__ uint32_t leaf_overflow(const DevGrid &g, uint32_t key) {
+// Inlined: as a call, the registers live across it spilled around the march
+// (measured: 132 -> 108 bytes of spill stores in k_pixel, +0.4% on 1080p frames).
+__device__ __forceinline__ uint32_t leaf_overflow(const DevGrid &g, uint32_t key) {
     uint32_t lo = 0, hi = g.n_ovf;
     while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
