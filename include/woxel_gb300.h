@@ -246,7 +246,7 @@ int wx_batch_destroy(wx_batch *batch);
  * caller must serialise them. The call blocks until earlier work on `stream`
  * is done, because the frame table is copied from pageable host memory. */
 #define WX_NOALLOC_MAX_FRAMES 256
-#define WX_NOALLOC_SCRATCH_BYTES 94464 /* 256 + 256 frames x 368-byte table entries */
+#define WX_NOALLOC_SCRATCH_BYTES 96512 /* 256 + 256 frames x 376-byte table entries */
 int wx_render_batch_noalloc(const wx_frame *frames, uint32_t n, void *stream);
 
 /* ---- serving: continuous batching of render requests (no counterpart in the
@@ -323,6 +323,15 @@ int wx_server_destroy(wx_server *srv);
  * division: every divisor m < max_m (<= 4096) and every significand of
  * [1,2) and [-2,-1). out = {mismatches, first bad m, its x bits}. */
 int wx_check_division(wx_ctx *ctx, uint32_t max_m, uint64_t out[3]);
+
+/* Bounds-checked build (libwoxel_gb300_checked.so, compiled with
+ * WX_BOUNDS_CHECK): every node-pool index the raycast kernels use and every
+ * pixel they write is compared with its pool or frame size; an index out of
+ * range is counted, never accessed (the ray ends), and no kernel traps. Returns
+ * in *count the number counted on the context's device since the last call and
+ * resets it, after waiting for the device. The normal build returns
+ * WX_ERR_UNSUPPORTED. */
+int wx_bounds_violations(wx_ctx *ctx, uint64_t *count);
 
 /* ---- host-side helpers (no GPU needed) ---- */
 /* ComputeState::build (compute_state.rs:87-131) for a look_at_rh camera

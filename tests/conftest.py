@@ -5,6 +5,7 @@ from pathlib import Path
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
+BOUNDS_CHECKED = os.environ.get("WOXEL_GB300_BOUNDS_CHECK") == "1"
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "oracle"))
 
@@ -15,10 +16,11 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session", autouse=True)
 def built_libraries():
-    """Build libwoxel_gb300.so and the oracle once per session (no-op when up to date)."""
+    """Build libwoxel_gb300.so (or, under WOXEL_GB300_BOUNDS_CHECK=1, the bounds-checked
+    build) and the oracle once per session (no-op when up to date)."""
     from woxel_gb300 import build as b
 
-    b.build()
+    b.build(checked=BOUNDS_CHECKED)
     b.build_oracle()
     yield
 
@@ -33,4 +35,6 @@ def cuda_ctx():
 
     ctx = wx.Context(int(os.environ.get("WX_TEST_DEVICE", "0")))
     yield ctx
+    if BOUNDS_CHECKED:  # every index the session's kernels used was in range
+        assert ctx.bounds_violations() == 0
     ctx.close()

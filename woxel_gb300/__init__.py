@@ -354,6 +354,13 @@ class Context:
         check(lib().wx_check_division(self._h, max_m, out), self._h)
         return int(out[0]), int(out[1]), int(out[2])
 
+    def bounds_violations(self) -> int:
+        """Out-of-range indices counted by the bounds-checked build (WOXEL_GB300_BOUNDS_CHECK=1)
+        since the last call; raises WxError in the normal build."""
+        n = C.c_uint64()
+        check(lib().wx_bounds_violations(self._h, C.byref(n)), self._h)
+        return int(n.value)
+
     @staticmethod
     def _frames(frames: Sequence) -> "C.Array":
         arr = (wx_frame * len(frames))()
@@ -384,7 +391,7 @@ def render_batch_noalloc(frames: Sequence, stream=None) -> None:
     """wx_render_batch_noalloc: a batch rendered without any allocation or context.
 
     For callers that cannot allocate device memory while rendering; scratch is a
-    fixed 94,464-byte device array inside the library (at most 256 frames a call).
+    fixed 96,512-byte device array inside the library (at most 256 frames a call).
     The first call on a device sets that device up; overlapping calls race.
     """
     arr = Context._frames(frames)

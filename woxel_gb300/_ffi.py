@@ -2,9 +2,12 @@
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "libwoxel_gb300.so"
+# WOXEL_GB300_BOUNDS_CHECK=1 loads the bounds-checked build instead (see wx_bounds_violations).
+LIB_PATH = Path(__file__).resolve().parent / (
+    "libwoxel_gb300_checked.so" if os.environ.get("WOXEL_GB300_BOUNDS_CHECK") == "1" else "libwoxel_gb300.so")
 
 WX_OK = 0
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "unsupported",
@@ -115,6 +118,7 @@ SIGNATURES = {
                                C.c_double]),
     "wx_server_destroy": (INT, [P]),
     "wx_check_division": (INT, [P, U32, C.POINTER(U64)]),
+    "wx_bounds_violations": (INT, [P, C.POINTER(U64)]),
     "wx_autotune": (INT, [P, C.POINTER(wx_frame), U32, C.POINTER(wx_tuning), U32, U32, C.POINTER(wx_tuning),
                           C.POINTER(C.c_double)]),
     "wx_state_build": (INT, [P, P, P, F32, F32, F32, U32, P, P, P, F32, C.POINTER(wx_state_uniform)]),

@@ -2,6 +2,9 @@
 
 The library is built in-tree as ``woxel_gb300/libwoxel_gb300.so``; object
 files go to ``woxel_gb300/_build/``. Translation units compile in parallel.
+``build(checked=True)`` builds ``libwoxel_gb300_checked.so`` with WX_BOUNDS_CHECK
+(every pool index and pixel the raycast kernels use is range-checked and counted,
+see wx_bounds_violations) from objects in ``woxel_gb300/_build/checked/``.
 """
 from __future__ import annotations
 
@@ -16,6 +19,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libwoxel_gb300.so"
+LIB_CHECKED = PKG / "libwoxel_gb300_checked.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no FMA contraction on the march (bit-exact FP32 op order);
@@ -48,20 +52,24 @@ def _stale(target: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False) -> Path:
-    """Compile every translation unit and link libwoxel_gb300.so. Returns its path."""
-    BUILD.mkdir(exist_ok=True)
-    inc = ["-I", str(ROOT / "include"), "-I", str(CSRC)]
+def build(verbose: bool = False, force: bool = False, checked: bool = False) -> Path:
+    """Compile every translation unit and link libwoxel_gb300.so (or, checked, the
+    bounds-checked libwoxel_gb300_checked.so). Returns its path."""
+    out_dir = BUILD / "checked" if checked else BUILD
+    lib = LIB_CHECKED if checked else LIB
+    defs = ["-DWX_BOUNDS_CHECK"] if checked else []
+    out_dir.mkdir(parents=True, exist_ok=True)
+    inc = ["-I", str(ROOT / "include"), "-I", str(CSRC), *defs]
     headers = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted((ROOT / "include").glob("*.h"))
     jobs = []
     objs = []
     for src in CU_SOURCES:
-        obj = BUILD / (Path(src).stem + ".o")
+        obj = out_dir / (Path(src).stem + ".o")
         objs.append(obj)
         if force or _stale(obj, [CSRC / src, *headers]):
             jobs.append([_nvcc(), *ARCH, *NVCC_FLAGS, *inc, "-c", str(CSRC / src), "-o", str(obj)])
     for src in CXX_SOURCES:
-        obj = BUILD / (Path(src).stem + ".o")
+        obj = out_dir / (Path(src).stem + ".o")
         objs.append(obj)
         if force or _stale(obj, [CSRC / src, *headers]):
             jobs.append(["g++", *CXX_FLAGS, *inc, *CUDA_INC, "-c", str(CSRC / src), "-o", str(obj)])
@@ -70,9 +78,9 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     if verbose:
         for o in outs:
             print(o)
-    if force or _stale(LIB, objs):
-        _run([_nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lpthread"])
-    return LIB
+    if force or _stale(lib, objs):
+        _run([_nvcc(), *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lpthread"])
+    return lib
 
 
 def build_oracle(verbose: bool = False) -> Path:
@@ -87,4 +95,5 @@ if __name__ == "__main__":
     import sys
 
     print(build(verbose="-v" in sys.argv, force="-f" in sys.argv))
+    print(build(verbose="-v" in sys.argv, force="-f" in sys.argv, checked=True))
     print(build_oracle())

@@ -276,6 +276,8 @@ int alloc_grid(wx_ctx *ctx, const std::vector<int4> &o5, uint64_t n5, uint64_t n
     gr->g.leaf = reinterpret_cast<const uint8_t *>(b + b_o5 + b5 + b4);
     gr->g.ovf = reinterpret_cast<const uint2 *>(b + b_o5 + b5 + b4 + b3);
     gr->g.n5 = (uint32_t)n5;
+    gr->g.n4 = (uint32_t)n4;
+    gr->g.n3 = (uint32_t)n3;
     gr->g.n_ovf = (uint32_t)n_ovf;
     gr->g.inside = 1u;
     for (uint64_t i = 0; i < n5; i++)
@@ -540,6 +542,21 @@ int wx_check_division(wx_ctx *ctx, uint32_t max_m, uint64_t out[3]) {
     WX_CUDA(ctx, cudaMemcpy(h, ctx->check, sizeof h, cudaMemcpyDeviceToHost));
     for (int i = 0; i < 3; i++) out[i] = h[i];
     return WX_OK;
+}
+
+int wx_bounds_violations(wx_ctx *ctx, uint64_t *count) {
+    if (!ctx || !count) return fail(ctx, WX_ERR_INVALID, "wx_bounds_violations: null argument");
+#ifdef WX_BOUNDS_CHECK
+    WX_CUDA(ctx, cudaSetDevice(ctx->device));
+    WX_CUDA(ctx, cudaDeviceSynchronize());
+    unsigned long long n = 0;
+    WX_CUDA(ctx, wxk::take_bounds_violations(&n));
+    *count = n;
+    return WX_OK;
+#else
+    *count = 0;
+    return fail(ctx, WX_ERR_UNSUPPORTED, "wx_bounds_violations: not a bounds-checked build");
+#endif
 }
 
 int wx_grid_build(wx_ctx *ctx, wx_topology *t, wx_grid **out) {

@@ -93,6 +93,7 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
     // disjoint from this frame's, the stores wait for it to complete. A no-op
     // in a launch that is not programmatically dependent.
     if (wait_prev) asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (!wx_in_range(pix, (uint64_t)J.width * J.height)) return;
     J.rgba[pix] = pack_rgba(c);
     if (J.hits)
         store_hit(J.hits + pix, hit.p, dot3(hit.p - eye, dir), hit.node,
@@ -271,6 +272,18 @@ bool all_modes(const Job *jobs, size_t n) {
     return false;
 }
 
+cudaError_t take_bounds_violations(unsigned long long *count) {
+#ifdef WX_BOUNDS_CHECK
+    cudaError_t e = cudaMemcpyFromSymbol(count, wxd::g_bounds_violations, sizeof *count);
+    if (e != cudaSuccess) return e;
+    const unsigned long long zero = 0;
+    return cudaMemcpyToSymbol(wxd::g_bounds_violations, &zero, sizeof zero);
+#else
+    *count = 0;
+    return cudaSuccess;
+#endif
+}
+
 cudaError_t check_division(uint32_t max_m, unsigned long long *out_dev, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(out_dev, 0, 3 * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
@@ -290,7 +303,7 @@ cudaError_t check_division(uint32_t max_m, unsigned long long *out_dev, cudaStre
 // deadline). wx_render_batch needs a context whose scratch (queue counters,
 // frame table) comes from cudaMalloc. This entry point instead keeps its
 // scratch in the fixed device array below, which the library declares
-// statically: every GPU that loads the library holds these 94,464 bytes until
+// statically: every GPU that loads the library holds these 96,512 bytes until
 // the process exits. Layout: the tile-queue counter at byte 0, the frame
 // (job) table from byte 256, room for WX_NOALLOC_MAX_FRAMES frames.
 // ---------------------------------------------------------------------------

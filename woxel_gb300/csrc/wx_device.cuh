@@ -32,6 +32,20 @@ using DevGrid = wxk::DevGrid;
 constexpr uint32_t kRcp = 4096;
 __device__ float g_rcp[kRcp];
 
+// Bounds-checked builds (WX_BOUNDS_CHECK): wx_in_range(i, n) is i < n; an index
+// out of range is counted in g_bounds_violations (read by wx_bounds_violations)
+// and the caller skips the access. Other builds compile the checks away.
+#ifdef WX_BOUNDS_CHECK
+__device__ unsigned long long g_bounds_violations;
+__device__ __forceinline__ bool wx_in_range(uint64_t i, uint64_t n) {
+    if (i < n) return true;
+    atomicAdd(&g_bounds_violations, 1ull);
+    return false;
+}
+#else
+__device__ __forceinline__ constexpr bool wx_in_range(uint64_t, uint64_t) { return true; }
+#endif
+
 __device__ __forceinline__ float pmin(float a, float b) { return (b < a || a != a) ? b : a; }
 __device__ __forceinline__ float pmax(float a, float b) { return (b > a || a != a) ? b : a; }
 __device__ __forceinline__ float sign11(float x) { return x < 0.0f ? -1.0f : 1.0f; }
@@ -206,6 +220,7 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
         }
     }
     if (lvl == 5) {  // get_vdb_leaf_from_node5 (:415-444)
+        if (!wx_in_range(r.i5, g.n5)) return 1u;
         const uint32_t off = ((((uint32_t)x >> 7) & 31u) << 10) | ((((uint32_t)y >> 7) & 31u) << 5) |
                              (((uint32_t)z >> 7) & 31u);
         const uint32_t w = __ldg(g.slot5 + ((r.i5 << 15) | off));
@@ -220,6 +235,7 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
         }
     }
     if (lvl == 4) {  // get_vdb_leaf_from_node4 (:446-475)
+        if (!wx_in_range(r.i4, g.n4)) return 1u;
         const uint32_t off = ((((uint32_t)x >> 3) & 15u) << 8) | ((((uint32_t)y >> 3) & 15u) << 4) |
                              (((uint32_t)z >> 3) & 15u);
         const uint32_t w = __ldg(g.slot4 + ((r.i4 << 12) | off));
@@ -234,6 +250,7 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
         }
     }
     if (lvl == 3) {  // get_vdb_leaf_from_node3 (:477-494)
+        if (!wx_in_range(r.i3, g.n3)) return 1u;
         const uint32_t key = (r.i3 << 9) | (((uint32_t)x & 7u) << 6) | (((uint32_t)y & 7u) << 3) | ((uint32_t)z & 7u);
         dist = __ldg(g.leaf + key);
         if (dist == 255u) dist = leaf_overflow(g, key);
@@ -539,9 +556,11 @@ __device__ __forceinline__ float surf_phi(const DevGrid &g, int i, int j, int k)
     const uint32_t w5 = __ldg(g.slot5 + ((n5 << 15) | ((((uint32_t)i >> 7) & 31u) << 10) |
                                          ((((uint32_t)j >> 7) & 31u) << 5) | (((uint32_t)k >> 7) & 31u)));
     if (!(w5 & kChild)) return w5 == 0u ? -g.band : g.band;
+    if (!wx_in_range(w5 & ~kChild, g.n4)) return g.band;
     const uint32_t w4 = __ldg(g.slot4 + (((w5 & ~kChild) << 12) | ((((uint32_t)i >> 3) & 15u) << 8) |
                                          ((((uint32_t)j >> 3) & 15u) << 4) | (((uint32_t)k >> 3) & 15u)));
     if (!(w4 & kChild)) return w4 == 0u ? -g.band : g.band;
+    if (!wx_in_range(w4 & ~kChild, g.n3)) return g.band;
     return __ldg(g.values + (((w4 & ~kChild) << 9) | (((uint32_t)i & 7u) << 6) | (((uint32_t)j & 7u) << 3) |
                              ((uint32_t)k & 7u)));
 }

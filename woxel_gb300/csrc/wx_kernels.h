@@ -20,6 +20,7 @@ struct DevGrid {
     uint32_t n5, n_ovf;
     float band;              // value of voxels outside leaves (+band; -band in active tiles)
     uint32_t inside;         // every N5 lies in [-4096, 4096)^3 (origins -4096 or 0 on each axis)
+    uint32_t n4, n3;         // node counts of the N4 and N3 pools (checked in bounds-checked builds)
 };
 
 // One frame of one grid: the unit the persistent kernels draw ray tiles from.
@@ -87,5 +88,7 @@ cudaError_t sdf_pack_leaves(const uint32_t *d, uint64_t ncells, uint8_t *leaf, u
 // every divisor m < max_m and every significand of [1,2) and [-2,-1).
 // out[0] = mismatch count, out[1] = first mismatching m, out[2] = its x bits.
 cudaError_t check_division(uint32_t max_m, unsigned long long *out_dev, cudaStream_t st);
+// Bounds-checked builds: reads and zeroes the device's count of out-of-range indices.
+cudaError_t take_bounds_violations(unsigned long long *count);
 
 }  // namespace wxk
