@@ -79,17 +79,12 @@ def replica_throughput(rays_per_rank: int, world: int, ms: float) -> float:
     return world * rays_per_rank / (ms / 1e3) / 1e9
 
 
-def profiled_traffic(kernel: str, workload: str):
-    """DRAM bytes (read + write) per launch from the committed ncu summary of this kernel and
-    workload (profiles/<kernel>_<workload>.md, line 'dram_bytes_per_launch: N'), else None."""
-    p = ROOT / "profiles" / f"{kernel}_{workload}.md"
-    try:
-        for line in p.read_text().splitlines():
-            if line.strip().startswith("dram_bytes_per_launch:"):
-                return float(line.split(":", 1)[1].strip().split()[0])
-    except OSError:
-        pass
-    return None
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
+# capture of the benchmark's kernel on each workload, with the commit it was taken on.
+# Reported as roofline.traffic_from_profile: a recorded capture, not a figure of this run.
+NCU_TRAFFIC = {
+    ("k_pixel", "spheres"): (142386432, "429288a"),
+}
 
 
 class ClockSampler:
@@ -147,99 +142,136 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------
-# CPU side: the oracle (restated reference algorithm) on a bounded tile sample.
+# CPU side: the oracle (restated reference algorithm) on tiles of the same frames.
 # --------------------------------------------------------------------------
-def sample_tiles(frame, fraction, rng):
-    tx, ty = frame.width // 8, frame.height // 4
-    n = tx * ty
-    k = max(1, int(n * fraction))
-    return np.sort(rng.choice(n, size=k, replace=False))
+def _oracle():
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as orc
+
+    return orc
 
 
-def oracle_sample(view, frames, fraction, nthreads, seed=5, stats=False):
-    """Render a random `fraction` of the 8x4 tiles of every frame on the CPU oracle.
+def tile_chunks(width: int, height: int, parts: int, seed: int) -> list:
+    """The 8x4 tiles of a frame in a seeded random order, split into `parts` chunks of equal
+    size (to one tile): chunk k of every frame is one step's sample, and `parts` consecutive
+    steps cover every tile once."""
+    n = (width // 8) * (height // 4)
+    perm = np.random.default_rng(seed).permutation(n)
+    return [np.sort(c) for c in np.array_split(perm, parts)]
+
+
+def oracle_sample(view, frames, chunk, parts, nthreads, seed=5, stats=False):
+    """Render chunk `chunk` of `parts` (tile_chunks) of every frame [(width, height, uniform
+    bytes)] on the CPU oracle.
 
     Returns (rays, seconds, mean node-visit bytes per primary ray incl. its shadow ray, grazing
     fraction of the primary rays); the last two only with stats=True."""
-    sys.path.insert(0, str(ROOT / "oracle"))
     import ctypes as C
 
-    import oracle as orc
-    import woxel_gb300 as wx
-
+    orc = _oracle()
     L = orc.lib()
     s, keep = orc._view_struct(view)
-    rng = np.random.default_rng(seed)
     rays, secs, byte_sum, grazing = 0, 0.0, 0.0, 0
-    for fr in frames:
-        st = fr.state()
-        sb = C.create_string_buffer(wx.state_bytes(st), 256)
-        tiles = sample_tiles(fr, fraction, rng)
-        rgba = np.zeros((fr.height, fr.width, 4), np.uint8)
-        stt = np.zeros((fr.height, fr.width), orc.STATS_DTYPE) if stats else None
+    for i, (w, h, sb_bytes) in enumerate(frames):
+        sb = C.create_string_buffer(sb_bytes, 256)
+        tiles = tile_chunks(w, h, parts, seed + i)[chunk % parts]
+        rgba = np.zeros((h, w, 4), np.uint8)
+        stt = np.zeros((h, w), orc.STATS_DTYPE) if stats else None
         tl = np.ascontiguousarray(tiles, np.uint64)
         t0 = time.perf_counter()
-        rc = L.orc_render_tile_list(C.byref(s), sb, fr.width, fr.height, tl.ctypes.data, tl.size, rgba.ctypes.data,
+        rc = L.orc_render_tile_list(C.byref(s), sb, w, h, tl.ctypes.data, tl.size, rgba.ctypes.data,
                                     None, None if stt is None else stt.ctypes.data, nthreads)
         secs += time.perf_counter() - t0
         if rc != 0:
             raise RuntimeError("oracle tile list out of range")
         rays += len(tiles) * 32
         if stats:
-            m = np.zeros((fr.height, fr.width), bool)
-            for t in tiles:
-                x0, y0 = (t % (fr.width // 8)) * 8, (t // (fr.width // 8)) * 4
-                m[y0:y0 + 4, x0:x0 + 8] = True
+            m = np.zeros((h // 4, w // 8), bool)
+            m.ravel()[tiles] = True
+            m = np.repeat(np.repeat(m, 4, axis=0), 8, axis=1)
+            m = np.pad(m, ((0, h - m.shape[0]), (0, w - m.shape[1])))
             byte_sum += float(stt["bytes"][m].sum() + stt["shadow_bytes"][m].sum())
             grazing += int(stt["grazing"][m].sum())
     del keep
     return rays, secs, (byte_sum / rays if stats else None), (grazing / rays if stats else None)
 
 
-def workload_label(name: str, frames) -> str:
-    """config.workload of both arms: the workload and its frames."""
-    return f"{name}: {len(frames)} x {frames[0].width}x{frames[0].height} frames, plain per-frame launches"
+def active_voxels(view) -> int:
+    """Active voxels of a view without active tiles: set bits of the leaf value masks."""
+    return int(np.unpackbits(np.ascontiguousarray(view["vals3"], np.uint32).view(np.uint8)).sum())
+
+
+def workload_config(name: str, counts, voxels: int, frames) -> dict:
+    """`config` of both arms: the workload, its grid and its frames [(width, height, ...)]."""
+    w, h = frames[0][0], frames[0][1]
+    mode = {"sphere": 3, "spheres": 3, "noise": 0}[name]
+    return {"workload": f"{name}: {len(frames)} x {w}x{h} frames, one plain per-frame raycast pass each",
+            "grid": {"n5": int(counts[0]), "n4": int(counts[1]), "n3": int(counts[2]), "active_voxels": int(voxels)},
+            "frames": len(frames), "resolution": f"{w}x{h}", "render_mode": mode}
 
 
 def run_reference(args, wl_name):
-    """--impl reference: the reference algorithm on the host cores (rank 0 only)."""
+    """--impl reference: the reference algorithm on the host cores (rank 0 only), built from
+    the oracle alone: the oracle's restated generator makes the grid through set_voxel, its
+    compute_sdf and atlas() flatten it, its ComputeState::build makes the uniforms, and its
+    restatement of raycast.comp.wgsl renders. No product code is loaded."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import woxel_gb300 as wx  # noqa: F401
-    from woxel_gb300 import workloads as W
-
-    wl = W.workload(wl_name)
-    topo = wl.grids[wl.frames[0].grid]()
-    view = topo.view()
+    orc = _oracle()
+    t0 = time.perf_counter()
+    view = orc.workload_view(wl_name)
+    t_view = time.perf_counter() - t0
+    frames = orc.workload_frames(wl_name)
+    counts = (view["kids5"].size // 1024, view["kids4"].size // 128, view["vals3"].size // 16)
     nthreads = os.cpu_count() or 1
-    frac = args.cpu_fraction
-    # warmup: one small sample
-    for _ in range(max(0, min(args.warmup, 1))):
-        oracle_sample(view, wl.frames[:1], frac / 4, nthreads, seed=99)
+    parts = max(1, int(round(1.0 / args.cpu_fraction)))
+    log(f"[reference] {wl_name}: grid {counts} built by the oracle in {t_view:.1f}s; {nthreads} threads")
+    for k in range(max(0, min(args.warmup, 1))):  # one warm-up step
+        oracle_sample(view, frames, k, parts * 4, nthreads, seed=99)
     times, rays_tot = [], 0
     for k in range(args.steps):
-        rays, secs, _, _ = oracle_sample(view, wl.frames, frac, nthreads, seed=100 + k)
+        rays, secs, _, _ = oracle_sample(view, frames, k, parts, nthreads, seed=100)
         times.append(secs)
         rays_tot += rays
     total = sum(times)
     value = rays_tot / total / 1e9
+    sample = (f"step k renders chunk k mod {parts} of a seeded split of each frame's 8x4 tiles into {parts} "
+              f"(every {parts} steps cover every tile of the {len(frames)} frames once); C restatement of "
+              f"raycast.comp.wgsl (oracle/), {nthreads} threads")
     line = {
         "impl": "reference", "metric": "primary_ray_grays_per_s", "value": value, "unit": "Grays/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload_label(wl_name, wl.frames),
-                   "grid": dict(zip(("n5", "n4", "n3"), topo.counts), active_voxels=topo.active_voxels),
-                   "render_mode": wl.frames[0].mode, "parallelism": f"cpu-threads x{nthreads}"},
-        "cpu_baseline": {"value": value, "unit": "Grays/s", "cores": nthreads, "kind": "port",
-                         "sample": f"{frac:.4f} of the 8x4 tiles of each of the {len(wl.frames)} frames per step, "
-                                   f"C restatement of raycast.comp.wgsl (oracle/), {nthreads} threads"},
+        "config": workload_config(wl_name, counts, active_voxels(view), frames),
+        "arm": {"parallelism": f"cpu-threads x{nthreads}", "grid_build_s": round(t_view, 2),
+                "grid_build": "oracle: restated generator + set_voxel, compute_sdf, masks(), atlas()",
+                "rays_per_step": rays_tot // max(1, args.steps)},
+        "cpu_baseline": {"value": value, "unit": "Grays/s", "cores": nthreads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "woxel's own pass (Rust + wgpu 0.17 CPU adapter) cannot run here: no Rust toolchain, "
                 "crates not vendored, no graphics stack; timed instead is the oracle's restatement",
     }
     print(json.dumps(line), flush=True)
+
+
+def traffic_from_profile(kernel: str, workload: str):
+    rec = NCU_TRAFFIC.get((kernel, workload))
+    if rec is None:
+        return None
+    return {"bytes_per_launch": rec[0], "capture_commit": rec[1],
+            "note": "ncu capture of one launch of this kernel on this workload (recorded, not this run)"}
+
+
+def roofline_view(name: str, topo):
+    """The view the oracle counts node-visit bytes on: built by the oracle alone (its
+    generator, compute_sdf and atlas()) for the sphere workloads; for the 2.7M-leaf noise
+    grid, whose single-threaded oracle SDF takes minutes, the product's masks and SDF
+    (equal to the oracle's word for word on the grid's first octant, tests/test_sdf_fullsize.py)."""
+    if name == "noise":
+        return topo.view(), "product SDF (oracle-equal on the first octant)"
+    return _oracle().workload_view(name), "oracle-built"
 
 
 # --------------------------------------------------------------------------
@@ -391,7 +423,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="spheres", choices=["sphere", "spheres", "noise"])
-    ap.add_argument("--cpu-fraction", type=float, default=1.0 / 8)
+    ap.add_argument("--cpu-fraction", type=float, default=None,
+                    help="fraction of each frame's tiles the CPU oracle renders per step (default: all of the "
+                         "640x480 frame, 1/8 of the 1080p frames, 1/32 of the 4K frames)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the mixed-load batched comparison")
@@ -411,6 +445,8 @@ def main():
     ap.add_argument("--tile-order", type=int, default=None, choices=[0, 1],
                     help="0 tile rows top to bottom, 1 middle rows first")
     args = ap.parse_args()
+    if args.cpu_fraction is None:
+        args.cpu_fraction = {"sphere": 1.0, "spheres": 1.0 / 8, "noise": 1.0 / 32}[args.workload]
     if args.impl == "reference":
         run_reference(args, args.workload)
         return
@@ -624,9 +660,14 @@ def main():
     kernel_name = "k_persistent" if ctx.tuning["kernel"] == 0 else "k_pixel"  # after autotuning
     if rank == 0:
         peak, peak_kind = hbm_peak()
-        view = topo.view()
+        t0 = time.perf_counter()
+        view, view_kind = roofline_view(args.workload, topo)
+        t_view = time.perf_counter() - t0
+        ofr = _oracle().workload_frames(args.workload)
+        assert all(wx.state_bytes(st) == o[2] for st, o in zip(states, ofr)), "uniforms differ from the oracle's"
         nthreads = os.cpu_count() or 1
-        rays_s, secs, bpr, grazing = oracle_sample(view, frames, args.cpu_fraction, nthreads, seed=5, stats=True)
+        parts = max(1, int(round(1.0 / args.cpu_fraction)))
+        rays_s, secs, bpr, grazing = oracle_sample(view, ofr, 0, parts, nthreads, seed=5, stats=True)
         # Launches overlap on the stream: a launch's share of the timed region is
         # the step time over its launches; one launch timed alone is also kept.
         launch_avg_ms = ms / len(frames)
@@ -639,7 +680,8 @@ def main():
                          "on them bit for bit (parity tests)"}
         l2 = l2_copy_peak(dev)
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": profiled_traffic(kernel_name, args.workload), "peak_kind": peak_kind,
+                "traffic": None, "traffic_from_profile": traffic_from_profile(kernel_name, args.workload),
+                "peak_kind": peak_kind, "view": view_kind, "view_build_s": round(t_view, 1),
                 "kernel": kernel_name, "algorithmic_bytes_per_ray": bpr,
                 "algorithmic_bytes_per_launch": bytes_launch, "launch_ms": launch_avg_ms,
                 "launch_alone": {"ms": launch_alone_ms, "achieved": bytes_launch / (launch_alone_ms / 1e3) / 1e9,
@@ -648,11 +690,11 @@ def main():
                        "peak_kind": "measured here: device copy between two L2-resident 32 MiB buffers"}}
         if not args.no_cpu:
             cpu = {"value": rays_s / secs / 1e9, "unit": "Grays/s", "cores": nthreads, "kind": "port",
-                   "sample": f"{args.cpu_fraction:.4f} of the 8x4 tiles of each of the {len(frames)} frames "
+                   "sample": f"1/{parts} of the 8x4 tiles of each of the {len(frames)} frames (seeded) "
                              f"({rays_s} rays), C restatement of raycast.comp.wgsl, {nthreads} threads"}
-            r1, s1, _, _ = oracle_sample(view, frames, args.cpu_fraction / 16, 1, seed=6)
+            r1, s1, _, _ = oracle_sample(view, ofr, 0, parts * 16, 1, seed=6)
             cpu["single_thread"] = {"value": r1 / s1 / 1e9, "unit": "Grays/s", "cores": 1,
-                                    "sample": f"{args.cpu_fraction / 16:.5f} of the tiles ({r1} rays)"}
+                                    "sample": f"1/{parts * 16} of the tiles ({r1} rays)"}
         del view
 
     if rank == 0:
@@ -660,14 +702,15 @@ def main():
             "metric": "primary_ray_grays_per_s", "value": value, "unit": "Grays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload_label(args.workload, frames),
-                       "grid": {k: info[k] for k in ("n5", "n4", "n3", "active_voxels", "device_bytes")},
-                       "grid_build_s": {"host_sdf": round(t_build, 3), "gpu_sdf": round(t_build_gpu, 3)},
-                       "render_mode": frames[0].mode, "l2": "flushed between steps (512 MB write)",
-                       "parallelism": f"replicas x{world}", "tuning": ctx.tuning,
-                       "autotune": tuned and {"table [kernel, tile_w, warps/block, blocks/SM (0 = all that fit), tile order (1 = middle rows first), ms for 4 frames]":
-                                              tuned["table"],
-                                              "seconds": tuned["seconds"]}},
+            "config": workload_config(args.workload, (info["n5"], info["n4"], info["n3"]), info["active_voxels"],
+                                      [(f.width, f.height) for f in frames]),
+            "arm": {"parallelism": f"replicas x{world}", "l2": "flushed between steps (512 MB write)",
+                    "device_bytes": info["device_bytes"],
+                    "grid_build_s": {"host_sdf": round(t_build, 3), "gpu_sdf": round(t_build_gpu, 3)},
+                    "tuning": ctx.tuning,
+                    "autotune": tuned and {"table [kernel, tile_w, warps/block, blocks/SM (0 = all that fit), tile order (1 = middle rows first), ms for 4 frames]":
+                                           tuned["table"],
+                                           "seconds": tuned["seconds"]}},
             "frame_latency_ms": {"p50": p50, "p99": p99},
             "batched_same_frames": same_batched, "batched": batched, "shadow_rays": shadow, "surface": surface,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "grazing_rays": graze,

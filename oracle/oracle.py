@@ -57,6 +57,14 @@ def lib() -> C.CDLL:
             "orc_render": (I, [P, P, C.c_uint32, C.c_uint32, P, P, P, I]),
             "orc_render_tiles": (I, [P, P, C.c_uint32, C.c_uint32, U64, U64, P, P, P, I]),
             "orc_render_tile_list": (I, [P, P, C.c_uint32, C.c_uint32, P, U64, P, P, P, I]),
+            "orc_sun_default": (None, [P, P, P]),
+            "orc_sphere_list": (None, [C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_float, U64, P]),
+            "orc_gen_spheres": (I, [P, P, C.c_uint32, C.c_double]),
+            "orc_set_leaf": (None, [P, P, P]),
+            "orc_gen_spheres_values": (I, [P, P, C.c_uint32, C.c_double, P]),
+            "orc_gen_noise_leaves": (C.c_int64, [P, C.c_int32, C.c_uint32, C.c_double, C.c_double, U64,
+                                                 C.c_int32, C.c_int32]),
+            "orc_orbit_eyes": (None, [C.c_uint32, C.c_float, U64, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -122,6 +130,35 @@ class Tree:
             raise ValueError("masks do not describe a consistent tree")
         return cls(h)
 
+    @classmethod
+    def spheres(cls, spheres: np.ndarray, band: float) -> "Tree":
+        """Narrow-band union of spheres (rows cx, cy, cz, r): every voxel with
+        |min_s(|ijk - c_s| - r_s)| < band set through set_voxel."""
+        t = cls()
+        sp = np.ascontiguousarray(spheres, np.float64).reshape(-1, 4)
+        if lib().orc_gen_spheres(t._h, sp.ctypes.data, sp.shape[0], float(band)) != 0:
+            raise MemoryError("orc_gen_spheres: out of memory")
+        return t
+
+    @classmethod
+    def noise_leaves(cls, lo: int, extent: int, occupancy: float, p_voxel: float, seed: int,
+                     box=None) -> "Tree":
+        """Value-noise leaves of [lo, lo + extent)^3; box=(b0, b1) keeps the leaves whose
+        origin lies in [b0, b1) on every axis."""
+        t = cls()
+        b0, b1 = box if box is not None else (0, 0)
+        if lib().orc_gen_noise_leaves(t._h, lo, extent, occupancy, p_voxel, seed, b0, b1) < 0:
+            raise ValueError("orc_gen_noise_leaves: bad arguments or out of memory")
+        return t
+
+    def spheres_values(self, spheres: np.ndarray, band: float) -> np.ndarray:
+        """Level-set values of every leaf voxel (n3 * 512 float32, DFS leaf order)."""
+        sp = np.ascontiguousarray(spheres, np.float64).reshape(-1, 4)
+        out = np.empty(self.counts[2] * 512, np.float32)
+        if lib().orc_gen_spheres_values(self._h, sp.ctypes.data, sp.shape[0], float(band), out.ctypes.data) != 0:
+            raise MemoryError("orc_gen_spheres_values: out of memory")
+        return out
+
     def set_voxel(self, p, value: int = 1) -> None:
         a = np.asarray(p, np.int32)
         lib().orc_set_voxel(self._h, a.ctypes.data, value)
@@ -156,9 +193,10 @@ class Tree:
         lib().orc_atlas(self._h, side.ctypes.data, a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data)
         return a, [int(s) for s in side]
 
-    def view(self) -> dict:
+    def view(self, sdf: bool = True) -> dict:
         """compute_sdf() then the flattened view (masks, origins, atlases)."""
-        self.compute_sdf()
+        if sdf:
+            self.compute_sdf()
         v = self.masks()
         a, s = self.atlas()
         v["atlas"] = a
@@ -172,6 +210,32 @@ def state_build(eye, target, up, aspect, fovy, width, mode, show_345, sun_dir, s
     lib().orc_state_build(f3(*eye), f3(*target), f3(*up), aspect, fovy, width, mode, (C.c_uint32 * 3)(*show_345),
                           f3(*sun_dir), f3(*sun_color), intensity, out)
     return out.raw
+
+
+def sun_default():
+    """(dir, colour, intensity) of the reference app's default sun (egui_dev.rs:355-368)."""
+    d, c, i = (C.c_float * 3)(), (C.c_float * 3)(), C.c_float()
+    lib().orc_sun_default(d, c, C.byref(i))
+    return tuple(d), tuple(c), i.value
+
+
+def sphere_list(count: int, rmin: float, rmax: float, lo: float, hi: float, seed: int) -> np.ndarray:
+    out = np.zeros((count, 4), np.float64)
+    lib().orc_sphere_list(count, rmin, rmax, lo, hi, seed, out.ctypes.data)
+    return out
+
+
+def orbit_eyes(count: int, radius: float, seed: int) -> np.ndarray:
+    out = np.zeros((count, 3), np.float32)
+    lib().orc_orbit_eyes(count, radius, seed, out.ctypes.data)
+    return out
+
+
+def frame_state(eye, width: int, height: int, mode: int, fovy: float = 60.0) -> bytes:
+    """Uniform of a camera at eye looking at the origin (up +y) with the default sun."""
+    sd, sc, si = sun_default()
+    return state_build(tuple(float(x) for x in eye), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), width / height, fovy,
+                       float(width), mode, (0, 0, 0), sd, sc, si)
 
 
 def _view_struct(v: dict):
@@ -220,3 +284,48 @@ def render(v: dict, state: bytes, width: int, height: int, nthreads: int = 1, hi
         raise RuntimeError(f"orc_render failed: {rc}")
     del keep
     return rgba, h, st
+
+
+# ---- The benchmark workloads, built by the oracle alone (no product code) ----
+# Same parameters as the product's seeded generators: one r=64 sphere at the origin;
+# 2000 spheres r ~ U[4,40], centres U[-1024,1024)^3, seed 2; value-noise leaves over
+# [-2048,2048)^3 at 2% occupancy, voxels p=0.5, seed 3; band 3 voxels.
+def workload_spheres(name: str) -> np.ndarray:
+    """Rows (cx, cy, cz, r) of the sphere workloads' spheres."""
+    if name == "sphere":
+        return np.array([[0.0, 0.0, 0.0, 64.0]])
+    if name == "spheres":
+        return sphere_list(2000, 4.0, 40.0, -1024.0, 1024.0, 2)
+    raise ValueError(f"{name!r} is not a sphere workload")
+
+
+def workload_tree(name: str, box=None) -> Tree:
+    if name in ("sphere", "spheres"):
+        return Tree.spheres(workload_spheres(name), 3.0)
+    if name == "noise":
+        return Tree.noise_leaves(-2048, 4096, 0.02, 0.5, 3, box)
+    raise ValueError(f"unknown workload {name!r}")
+
+
+def workload_frames(name: str) -> list:
+    """[(width, height, uniform bytes)] of the workload's cameras: the 640x480 view from
+    (0,0,200); 16 orbit eyes at radius 3000 (seed 16), 1920x1080, Lambert mode 3; 8 orbit
+    eyes at radius 3500 (seed 8), 3840x2160, mode 0. All 60 degree, looking at the origin."""
+    if name == "sphere":
+        return [(640, 480, frame_state((0.0, 0.0, 200.0), 640, 480, 3))]
+    if name == "spheres":
+        return [(1920, 1080, frame_state(e, 1920, 1080, 3)) for e in orbit_eyes(16, 3000.0, 16)]
+    if name == "noise":
+        return [(3840, 2160, frame_state(e, 3840, 2160, 0)) for e in orbit_eyes(8, 3500.0, 8)]
+    raise ValueError(f"unknown workload {name!r}")
+
+
+def workload_view(name: str, box=None, values: bool = False) -> dict:
+    """The workload's flattened view (compute_sdf, masks, atlas) built by the oracle; with
+    values=True (sphere workloads) also its level-set values and band for render mode 5."""
+    t = workload_tree(name, box)
+    v = t.view()
+    if values:
+        v["values"], v["band"] = t.spheres_values(workload_spheres(name), 3.0), 3.0
+    del t
+    return v

@@ -1227,3 +1227,358 @@ int orc_render(const orc_view *v, const orc_state *s, uint32_t width, uint32_t h
                uint8_t *rgba, orc_hit *hits, orc_stats *stats, int nthreads) {
     return orc_render_tiles(v, s, width, height, 0, UINT64_MAX, rgba, hits, stats, nthreads);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Synthetic workloads. The reference reads its grids from .vdb files and has */
+/* no generator; these are the benchmark's seeded stand-ins, stated here once */
+/* more so that a CPU run (the reference arm of the benchmark, the parity     */
+/* tests) can build its grid, cameras and uniforms without the product:       */
+/*   splitmix64 (Steele, Lea & Flood 2014) as the seeded stream;              */
+/*   narrow-band spheres: voxel ijk active iff |min_s(|ijk - c_s| - r_s)| <   */
+/*     band, in double precision, set through set_voxel (vdb345.rs:26-66);    */
+/*   3-octave value noise on the leaf lattice, thresholded to an occupancy;   */
+/*   orbit eyes uniform on the sphere with |y| <= 0.9 radius.                 */
+/* ------------------------------------------------------------------------ */
+static uint64_t sm64_next(uint64_t *s) {
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static double sm64_uniform(uint64_t *s) { return (double)(sm64_next(s) >> 11) * 0x1.0p-53; }
+static uint64_t hash2(uint64_t a, uint64_t b) {
+    uint64_t s = (a * 0xD6E8FEB86659FD93ull) ^ (b + 0x632BE59BD9B4E019ull);
+    return sm64_next(&s);
+}
+
+/* Sun defaults of the reference app (egui_dev.rs:355-368): glam's
+ * Vec3::normalize is v * (1 / sqrt((x*x + y*y) + z*z)). */
+void orc_sun_default(float dir[3], float color[3], float *intensity) {
+    const float v[3] = {1.0f, -1.0f, 0.5f};
+    const float r = 1.0f / sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+    for (int i = 0; i < 3; i++) dir[i] = v[i] * r;
+    color[0] = 255.0f / 255.0f;
+    color[1] = 210.0f / 255.0f;
+    color[2] = 160.0f / 255.0f;
+    *intensity = 1.0f;
+}
+
+void orc_sphere_list(uint32_t count, float rmin, float rmax, float lo, float hi, uint64_t seed,
+                     double *out) {
+    uint64_t s = seed;
+    const float span = hi - lo, rspan = rmax - rmin; /* single-precision differences */
+    for (uint32_t i = 0; i < count; i++) { /* per sphere: cx, cy, cz, then r */
+        for (int a = 0; a < 3; a++) out[4 * i + a] = (double)lo + (double)span * sm64_uniform(&s);
+        out[4 * i + 3] = (double)rmin + (double)rspan * sm64_uniform(&s);
+    }
+}
+
+static double sphere_dist(const double *q, int32_t x, int32_t y, int32_t z) {
+    const double dx = (double)x - q[0], dy = (double)y - q[1], dz = (double)z - q[2];
+    return sqrt(dx * dx + dy * dy + dz * dz) - q[3];
+}
+
+/* Every voxel whose |signed distance to the union| is below band becomes active.
+ * A voxel can only be active through a sphere whose shell (|d_s| < band) holds it,
+ * so each sphere's bounding box is scanned for its own shell voxels, and for those
+ * the union distance is taken over every sphere whose box (c +- (r + band)) covers
+ * a 64-voxel cell around it. Returns 0, or 1 when an allocation fails. */
+int orc_gen_spheres(orc_tree *t, const double *sph, uint32_t count, double band) {
+    if (!count) return 0;
+    enum { C = 64 };
+    double blo[3] = {INFINITY, INFINITY, INFINITY}, bhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = 0; i < count; i++)
+        for (int a = 0; a < 3; a++) {
+            blo[a] = fmin(blo[a], floor(sph[4 * i + a] - sph[4 * i + 3] - band));
+            bhi[a] = fmax(bhi[a], ceil(sph[4 * i + a] + sph[4 * i + 3] + band));
+        }
+    int64_t c0[3], nc[3];
+    for (int a = 0; a < 3; a++) {
+        c0[a] = (int64_t)floor(blo[a] / C);
+        nc[a] = (int64_t)floor(bhi[a] / C) - c0[a] + 1;
+    }
+    const size_t ncell = (size_t)(nc[0] * nc[1] * nc[2]);
+    /* Cell lists in CSR form: start[c] .. start[c + 1] index ids. */
+    size_t *start = calloc(ncell + 1, sizeof(size_t));
+    if (!start) return 1;
+    uint32_t *ids = NULL;
+    for (int pass = 0; pass < 2; pass++) {
+        if (pass == 1) {
+            for (size_t c = 0; c < ncell; c++) start[c + 1] += start[c];
+            ids = malloc(sizeof(uint32_t) * (start[ncell] ? start[ncell] : 1));
+            if (!ids) { free(start); return 1; }
+        }
+        for (uint32_t i = 0; i < count; i++) {
+            int64_t lc[3], hc[3];
+            for (int a = 0; a < 3; a++) {
+                lc[a] = (int64_t)floor(floor(sph[4 * i + a] - sph[4 * i + 3] - band) / C) - c0[a];
+                hc[a] = (int64_t)floor(ceil(sph[4 * i + a] + sph[4 * i + 3] + band) / C) - c0[a];
+            }
+            for (int64_t x = lc[0]; x <= hc[0]; x++)
+                for (int64_t y = lc[1]; y <= hc[1]; y++)
+                    for (int64_t z = lc[2]; z <= hc[2]; z++) {
+                        const size_t c = (size_t)((x * nc[1] + y) * nc[2] + z);
+                        if (pass == 0) start[c + 1]++;
+                        else ids[start[c]++] = i; /* advances start[c] to cell c's end */
+                    }
+        }
+    }
+    /* After the fill start[c] is the end of cell c's list, so cell c spans
+     * [c ? start[c - 1] : 0, start[c]). */
+    for (uint32_t i = 0; i < count; i++) {
+        const double *q = sph + 4 * i;
+        int32_t lv[3], hv[3];
+        for (int a = 0; a < 3; a++) {
+            lv[a] = (int32_t)floor(q[a] - q[3] - band);
+            hv[a] = (int32_t)ceil(q[a] + q[3] + band);
+        }
+        for (int32_t x = lv[0]; x <= hv[0]; x++)
+            for (int32_t y = lv[1]; y <= hv[1]; y++)
+                for (int32_t z = lv[2]; z <= hv[2]; z++) {
+                    if (!(fabs(sphere_dist(q, x, y, z)) < band)) continue;
+                    const int64_t cx = (int64_t)floor((double)x / C) - c0[0];
+                    const int64_t cy = (int64_t)floor((double)y / C) - c0[1];
+                    const int64_t cz = (int64_t)floor((double)z / C) - c0[2];
+                    const size_t c = (size_t)((cx * nc[1] + cy) * nc[2] + cz);
+                    double d = INFINITY;
+                    for (size_t k = c ? start[c - 1] : 0; k < start[c]; k++)
+                        d = fmin(d, sphere_dist(sph + 4 * ids[k], x, y, z));
+                    if (fabs(d) < band) {
+                        const int32_t p[3] = {x, y, z};
+                        orc_set_voxel(t, p, 1);
+                    }
+                }
+    }
+    free(ids);
+    free(start);
+    return 0;
+}
+
+/* Level-set values of a sphere union for every voxel of every leaf of t (DFS leaf order,
+ * voxel x<<6 | y<<3 | z): the signed distance min_s(|ijk - c_s| - r_s) clamped to
+ * [-band, band], as a narrow-band level set stores it. The minimum runs over the spheres
+ * whose box c +- (r + band) meets the leaf; any other sphere is farther than band from
+ * every voxel of the leaf, so it cannot change the clamped value. 0, or 1 (no memory). */
+int orc_gen_spheres_values(const orc_tree *t, const double *sph, uint32_t count, double band, float *out) {
+    uint32_t *ids = malloc(sizeof(uint32_t) * (count ? count : 1));
+    if (!ids) return 1;
+    size_t leaf = 0;
+    for (size_t r = 0; r < t->nroots; r++) {
+        const ON5 *n5 = t->n5[t->roots[r].n5];
+        const int32_t *key = t->roots[r].key;
+        for (int o5 = 0; o5 < 32768; o5++) {
+            if (n5->child[o5] < 0) continue;
+            const ON4 *n4 = t->n4[n5->child[o5]];
+            uint32_t c5[3];
+            orc_offset_to_child((uint64_t)o5, 5, c5);
+            for (int o4 = 0; o4 < 4096; o4++) {
+                if (n4->child[o4] < 0) continue;
+                uint32_t c4[3];
+                orc_offset_to_child((uint64_t)o4, 4, c4);
+                int32_t org[3];
+                for (int a = 0; a < 3; a++) org[a] = key[a] + (int32_t)c5[a] * 128 + (int32_t)c4[a] * 8;
+                uint32_t nid = 0;
+                for (uint32_t i = 0; i < count; i++) {
+                    const double *q = sph + 4 * i;
+                    int meets = 1;
+                    for (int a = 0; a < 3 && meets; a++)
+                        meets = floor(q[a] - q[3] - band) <= (double)(org[a] + 7) &&
+                                ceil(q[a] + q[3] + band) >= (double)org[a];
+                    if (meets) ids[nid++] = i;
+                }
+                for (int v = 0; v < 512; v++) {
+                    const int32_t x = org[0] + (v >> 6), y = org[1] + ((v >> 3) & 7), z = org[2] + (v & 7);
+                    double d = INFINITY;
+                    for (uint32_t k = 0; k < nid; k++) d = fmin(d, sphere_dist(sph + 4 * ids[k], x, y, z));
+                    out[leaf * 512 + (size_t)v] = (float)fmin(band, fmax(-band, d));
+                }
+                leaf++;
+            }
+        }
+    }
+    free(ids);
+    return 0;
+}
+
+/* set_voxel(p, 1) for every set bit of a leaf's 512-bit mask (bit x<<6 | y<<3 | z):
+ * the nodes on the way are created and marked as set_voxel (vdb345.rs:26-66) does for
+ * the leaf's first voxel, then the leaf's value bits are or-ed in. */
+void orc_set_leaf(orc_tree *t, const int32_t origin[3], const uint64_t mask[8]) {
+    int first = -1;
+    for (int w = 0; w < 8 && first < 0; w++)
+        if (mask[w]) first = 64 * w + __builtin_ctzll(mask[w]);
+    if (first < 0) return;
+    const int32_t p[3] = {origin[0] + (first >> 6), origin[1] + ((first >> 3) & 7), origin[2] + (first & 7)};
+    orc_set_voxel(t, p, 1);
+    int32_t key[3];
+    orc_global_to_node(p, 12, key);
+    const ON5 *n5 = t->n5[t->roots[root_find(t, key, NULL)].n5];
+    const ON4 *n4 = t->n4[n5->child[orc_global_to_offset(p, 5, 12)]];
+    ON3 *n3 = t->n3[n4->child[orc_global_to_offset(p, 4, 7)]];
+    for (int v = 0; v < 512; v++) {
+        if (!((mask[v >> 6] >> (v & 63)) & 1)) continue;
+        n3->val[v >> 6] |= 1ull << (v & 63);
+        n3->is_value[v] = 1;
+        n3->value[v] = 1;
+    }
+}
+
+/* Value noise: octave k has 8 << k cells over the n-leaf lattice; corner values
+ * are (hash >> 40) * 2^-24 in [0, 1); smoothstep weights; amplitudes 1, 1/2, 1/4.
+ * All arithmetic single precision except the corner draw. */
+static float noise_at(float *const corners[3], int n, int lx, int ly, int lz) {
+    float sum = 0.0f, amp = 1.0f;
+    for (int k = 0; k < 3; k++) {
+        const int cells = 8 << k, c = cells + 1;
+        const float scale = (float)cells / (float)n;
+        const float u[3] = {((float)lx + 0.5f) * scale, ((float)ly + 0.5f) * scale, ((float)lz + 0.5f) * scale};
+        int i0[3];
+        float w[3];
+        for (int a = 0; a < 3; a++) {
+            int fl = (int)floorf(u[a]);
+            i0[a] = fl < cells - 1 ? fl : cells - 1;
+            const float f = u[a] - (float)i0[a];
+            w[a] = f * f * (3.0f - 2.0f * f);
+        }
+#define G(dx, dy, dz) corners[k][((size_t)(i0[0] + (dx)) * c + (size_t)(i0[1] + (dy))) * c + (size_t)(i0[2] + (dz))]
+        const float x00 = G(0, 0, 0) + w[0] * (G(1, 0, 0) - G(0, 0, 0));
+        const float x10 = G(0, 1, 0) + w[0] * (G(1, 1, 0) - G(0, 1, 0));
+        const float x01 = G(0, 0, 1) + w[0] * (G(1, 0, 1) - G(0, 0, 1));
+        const float x11 = G(0, 1, 1) + w[0] * (G(1, 1, 1) - G(0, 1, 1));
+#undef G
+        const float y0 = x00 + w[1] * (x10 - x00), y1 = x01 + w[1] * (x11 - x01);
+        sum += amp * (y0 + w[2] * (y1 - y0));
+        amp *= 0.5f;
+    }
+    return sum;
+}
+
+/* Noise value of every lattice leaf, x-major; x-slabs spread over threads (each value
+ * depends only on its own coordinates). */
+typedef struct {
+    float *const *corners;
+    float *val;
+    int n;
+    atomic_int next;
+} NoiseJob;
+static void *noise_worker(void *arg) {
+    NoiseJob *j = (NoiseJob *)arg;
+    for (;;) {
+        const int x = atomic_fetch_add(&j->next, 1);
+        if (x >= j->n) break;
+        for (int y = 0; y < j->n; y++)
+            for (int z = 0; z < j->n; z++)
+                j->val[((size_t)x * j->n + y) * j->n + z] = noise_at(j->corners, j->n, x, y, z);
+    }
+    return NULL;
+}
+static void noise_fill(float *const corners[3], int n, float *val) {
+    NoiseJob j = {corners, val, n, 0};
+    enum { T = 16 };
+    pthread_t th[T];
+    int started = 0;
+    for (; started < T; started++)
+        if (pthread_create(&th[started], NULL, noise_worker, &j) != 0) break;
+    noise_worker(&j);
+    for (int i = 0; i < started; i++) pthread_join(th[i], NULL);
+}
+
+/* k-th smallest of a[0..n) (0-based); reorders a. Hoare partition, middle pivot. */
+static float select_kth(float *a, size_t n, size_t k) {
+    size_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const float piv = a[lo + (hi - lo) / 2];
+        size_t i = lo, j = hi;
+        while (i <= j) {
+            while (a[i] < piv) i++;
+            while (a[j] > piv) j--;
+            if (i <= j) {
+                float tmp = a[i]; a[i] = a[j]; a[j] = tmp;
+                i++;
+                if (j == 0) break;
+                j--;
+            }
+        }
+        if (k <= j) hi = j;
+        else if (k >= i) lo = i;
+        else return a[k];
+    }
+    return a[k];
+}
+
+/* Leaves of [lo, lo + extent)^3 whose noise value exceeds the value with exactly
+ * round(occupancy * leaves) leaves above it; voxels of a kept leaf active with
+ * probability p_voxel (p = 0.5: the raw hash bits). Only leaves whose origin lies in
+ * [box_lo, box_hi) on every axis are set (the whole domain when box_lo >= box_hi).
+ * Returns the number of leaves kept in the whole domain, or -1 on a bad argument or
+ * a failed allocation. */
+int64_t orc_gen_noise_leaves(orc_tree *t, int32_t lo, uint32_t extent, double occupancy, double p_voxel,
+                             uint64_t seed, int32_t box_lo, int32_t box_hi) {
+    if (extent < 64 || (extent & 7) || !(occupancy > 0.0 && occupancy < 1.0) || (lo & 7)) return -1;
+    const int n = (int)(extent / 8);
+    const size_t total = (size_t)n * n * n;
+    float *corners[3] = {NULL, NULL, NULL};
+    for (int k = 0; k < 3; k++) {
+        const int c = (8 << k) + 1;
+        corners[k] = malloc(sizeof(float) * (size_t)c * c * c);
+        if (!corners[k]) goto oom;
+        for (int x = 0; x < c; x++)
+            for (int y = 0; y < c; y++)
+                for (int z = 0; z < c; z++) {
+                    uint64_t h = hash2(seed ^ (0x1000193ull * (uint64_t)(k + 1)),
+                                       ((uint64_t)x << 42) | ((uint64_t)y << 21) | (uint64_t)z);
+                    corners[k][((size_t)x * c + y) * c + z] = (float)((double)(h >> 40) * 0x1.0p-24);
+                }
+    }
+    float *val = malloc(sizeof(float) * total), *tmp = malloc(sizeof(float) * total);
+    if (!val || !tmp) { free(val); free(tmp); goto oom; }
+    noise_fill(corners, n, val);
+    const size_t keep = (size_t)llround(occupancy * (double)total);
+    memcpy(tmp, val, sizeof(float) * total);
+    const float thr = select_kth(tmp, total, total - keep - (keep < total ? 1 : 0));
+    free(tmp);
+    int64_t kept = 0;
+    for (size_t i = 0; i < total; i++) {
+        if (!(val[i] > thr)) continue;
+        kept++;
+        const int32_t o[3] = {lo + 8 * (int32_t)(i / ((size_t)n * n)), lo + 8 * (int32_t)((i / n) % n),
+                              lo + 8 * (int32_t)(i % n)};
+        if (box_lo < box_hi && (o[0] < box_lo || o[0] >= box_hi || o[1] < box_lo || o[1] >= box_hi ||
+                                o[2] < box_lo || o[2] >= box_hi))
+            continue;
+        uint64_t m[8];
+        for (int w = 0; w < 8; w++) {
+            const uint64_t h = hash2(seed ^ 0xA5A5A5A5DEADBEEFull, (uint64_t)i * 8 + (uint64_t)w);
+            if (p_voxel == 0.5) {
+                m[w] = h;
+            } else {
+                uint64_t s = h, b = 0;
+                for (int k = 0; k < 64; k++)
+                    if (sm64_uniform(&s) < p_voxel) b |= 1ull << k;
+                m[w] = b;
+            }
+        }
+        orc_set_leaf(t, o, m);
+    }
+    free(val);
+    for (int k = 0; k < 3; k++) free(corners[k]);
+    return kept;
+oom:
+    for (int k = 0; k < 3; k++) free(corners[k]);
+    return -1;
+}
+
+void orc_orbit_eyes(uint32_t count, float radius, uint64_t seed, float *eyes) {
+    uint64_t s = seed;
+    for (uint32_t i = 0; i < count; i++) {
+        double y;
+        do {
+            y = 2.0 * sm64_uniform(&s) - 1.0;
+        } while (fabs(y) > 0.9);
+        const double phi = 2.0 * 3.14159265358979323846 * sm64_uniform(&s);
+        const double r = sqrt(1.0 - y * y);
+        eyes[3 * i + 0] = (float)(radius * r * cos(phi));
+        eyes[3 * i + 1] = (float)(radius * y);
+        eyes[3 * i + 2] = (float)(radius * r * sin(phi));
+    }
+}

@@ -125,6 +125,31 @@ void orc_state_build(const float eye[3], const float target[3], const float up[3
                      const float sun_dir[3], const float sun_color[3], float sun_intensity,
                      orc_state *out);
 
+/* ---- synthetic workloads (no reference counterpart: the benchmark's seeded grids,
+ * cameras and sun, stated independently of the product so that a CPU run can build
+ * them alone). splitmix64 is the seeded stream. ---- */
+/* Sun defaults of the reference app (egui_dev.rs:355-368). */
+void orc_sun_default(float dir[3], float color[3], float *intensity);
+/* count spheres drawn as cx, cy, cz in lo + (hi - lo) * U and r in rmin + (rmax - rmin) * U;
+ * out holds count * 4 doubles (cx, cy, cz, r). */
+void orc_sphere_list(uint32_t count, float rmin, float rmax, float lo, float hi, uint64_t seed,
+                     double *out);
+/* set_voxel(ijk, 1) for every voxel with |min_s(|ijk - c_s| - r_s)| < band. 0 or 1 (no memory). */
+int orc_gen_spheres(orc_tree *t, const double *spheres, uint32_t count, double band);
+/* Level-set values (n3 * 512 floats, DFS leaf order, voxel x<<6 | y<<3 | z) of the sphere
+ * union: min_s(|ijk - c_s| - r_s) clamped to [-band, band]. 0 or 1 (no memory). */
+int orc_gen_spheres_values(const orc_tree *t, const double *spheres, uint32_t count, double band, float *out);
+/* set_voxel(origin + (v >> 6, v >> 3 & 7, v & 7), 1) for every set bit v of mask. */
+void orc_set_leaf(orc_tree *t, const int32_t origin[3], const uint64_t mask[8]);
+/* 3-octave value-noise leaves of [lo, lo + extent)^3 at the given occupancy, voxels
+ * active with probability p_voxel; only leaves with every origin coordinate in
+ * [box_lo, box_hi) are set (all when box_lo >= box_hi). Returns the leaves kept in the
+ * whole domain, -1 on bad arguments or no memory. */
+int64_t orc_gen_noise_leaves(orc_tree *t, int32_t lo, uint32_t extent, double occupancy, double p_voxel,
+                             uint64_t seed, int32_t box_lo, int32_t box_hi);
+/* count eyes uniform on the sphere of the given radius, |y| <= 0.9 radius (float x, y, z). */
+void orc_orbit_eyes(uint32_t count, float radius, uint64_t seed, float *eyes);
+
 /* ---- the raycast pass (raycast.comp.wgsl:60-519) ---- */
 /* Renders the (8*floor(W/8)) x (4*floor(H/4)) pixels the dispatch covers.
  * rgba: W*H*4 bytes (row-major, y*W + x); hits/stats may be NULL.

@@ -38,3 +38,13 @@ def cuda_ctx():
     if BOUNDS_CHECKED:  # every index the session's kernels used was in range
         assert ctx.bounds_violations() == 0
     ctx.close()
+
+
+@pytest.fixture(scope="session")
+def oracle_spheres_view():
+    """The 2000-sphere benchmark grid's flattened view with its level-set values, built by
+    the oracle alone (restated generator, set_voxel, compute_sdf, atlas()): the view the
+    full-size parity tests hand the oracle, independent of the product's generator and SDF."""
+    import oracle as orc
+
+    return orc.workload_view("spheres", values=True)

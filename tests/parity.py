@@ -36,6 +36,13 @@ def gpu_render(ctx, grid, state, width, height, hits=True, host=False):
     return rgba, h
 
 
+def oracle_view(topo) -> dict:
+    """The view the oracle renders for a product topology: its masks (the grid's input,
+    which the oracle's own generators reproduce bit for bit) flattened by the oracle's
+    compute_sdf and atlas(), so that no parity test hands the oracle the product's SDF."""
+    return orc.Tree.from_masks(topo.masks()).view()
+
+
 def oracle_render(view, state, width, height, nthreads=8, tiles=None):
     return orc.render(view, wx.state_bytes(state), width, height, nthreads=nthreads, hits=True, tiles=tiles)[:2]
 

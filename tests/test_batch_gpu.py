@@ -8,7 +8,7 @@ import pytest
 import torch
 
 import woxel_gb300 as wx
-from parity import compare, dispatch_mask, gpu_render, oracle_render
+from parity import compare, dispatch_mask, gpu_render, oracle_render, oracle_view
 
 pytestmark = pytest.mark.gpu
 
@@ -18,7 +18,7 @@ def scene(cuda_ctx):
     rng = np.random.default_rng(21)
     t1 = wx.Topology.sphere((0, 0, 0), 64.0, 3.0)
     t2 = wx.Topology.from_voxels(rng.integers(-300, 300, size=(4000, 3)).astype(np.int32))
-    views = [t1.view(), t2.view()]
+    views = [oracle_view(t1), oracle_view(t2)]
     grids = [cuda_ctx.build_grid(t1), cuda_ctx.build_grid(t2)]
     frames = []
     sizes = [(64, 48), (120, 64), (96, 96), (33, 17), (160, 120), (8, 4), (7, 3), (200, 52)]

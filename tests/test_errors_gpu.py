@@ -5,7 +5,7 @@ import pytest
 import torch
 
 import woxel_gb300 as wx
-from parity import compare, gpu_render, oracle_render
+from parity import compare, gpu_render, oracle_render, oracle_view
 
 pytestmark = pytest.mark.gpu
 
@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture(scope="module")
 def sphere(cuda_ctx):
     topo = wx.Topology.sphere((0, 0, 0), 40.0, 3.0)
-    return topo, topo.view(), cuda_ctx.build_grid(topo)
+    return topo, oracle_view(topo), cuda_ctx.build_grid(topo)
 
 
 def state(w=64, h=48, mode=3):

@@ -1,9 +1,17 @@
 """Parity at the benchmark's full sizes, on sampled tiles and size-independent properties.
 
+The oracle side is built by the oracle alone: its restated generator sets the voxels,
+its compute_sdf and atlas() flatten the grid, its ComputeState::build makes the
+uniforms (asserted byte-equal to the product's). The GPU side is the product's
+generator, SDF, pools and kernels.
+
 * 2000-sphere grid (476k leaves), 1920x1080 frames: random 8x4 tiles against the
-  oracle; batched launch == per-frame launches; repeated renders identical.
-* 4096^3 noise grid (2.68M leaves, 2% occupancy, p=0.5 voxels), 3840x2160, mode 0
-  (first active voxel): random tiles against the oracle.
+  oracle-built view; batched launch == per-frame launches; repeated renders identical.
+* noise grid, 3840x2160, mode 0 (first active voxel): the [-2048,0)^3 octant of the
+  benchmark's 4096^3 grid (367,660 leaves) against the oracle-built view of that octant;
+  and the whole 2.68M-leaf grid against the oracle marching over the product's flattened
+  view (the march at full size; the SDF of the whole grid takes the single-threaded oracle
+  minutes, so the octant carries the independent SDF check).
 """
 import numpy as np
 import pytest
@@ -26,29 +34,36 @@ def tile_mask(w, h, tiles):
     return m
 
 
-def sampled_parity(ctx, grid, view, frame, ntiles, seed):
+def sampled_parity(ctx, grid, view, frame, ntiles, seed, oracle_state=None):
+    """GPU frame vs the oracle on `ntiles` random tiles; the oracle renders with its own
+    uniform (oracle_state) when given, which must equal the product's byte for byte."""
     st = frame.state()
+    sb = wx.state_bytes(st)
+    if oracle_state is not None:
+        assert oracle_state == sb, "uniform differs from the oracle's"
+        sb = oracle_state
     rg, hg = gpu_render(ctx, grid, st, frame.width, frame.height)
     rng = np.random.default_rng(seed)
     tiles = np.sort(rng.choice((frame.width // 8) * (frame.height // 4), size=ntiles, replace=False)).astype(np.uint64)
-    ro, ho, _ = orc.render(view, wx.state_bytes(st), frame.width, frame.height, nthreads=16, hits=True, tiles=tiles)
+    ro, ho, _ = orc.render(view, sb, frame.width, frame.height, nthreads=16, hits=True, tiles=tiles)
     m = tile_mask(frame.width, frame.height, tiles)
     compare(rg, hg, ro, ho, where=m, label=f"{frame.grid} {frame.width}x{frame.height}")
     return rg, hg
 
 
 @pytest.fixture(scope="module")
-def spheres(cuda_ctx):
+def spheres(cuda_ctx, oracle_spheres_view):
     topo = W.spheres_topology()
     grid = cuda_ctx.build_grid(topo)
-    return topo, topo.view(), grid
+    return topo, oracle_spheres_view, grid
 
 
 def test_spheres_1080p_sampled_tiles(cuda_ctx, spheres):
     topo, view, grid = spheres
     frames = W.spheres_frames()
-    for k in (0, 7):
-        rg, hg = sampled_parity(cuda_ctx, grid, view, frames[k], ntiles=1500, seed=k)
+    ostates = orc.workload_frames("spheres")
+    for k in (0, 7, 12):
+        rg, hg = sampled_parity(cuda_ctx, grid, view, frames[k], ntiles=1500, seed=k, oracle_state=ostates[k][2])
         assert (wx.hit_fields(hg)["state"] == 0).mean() > 0.05
 
 
@@ -84,6 +99,25 @@ def test_spheres_all_kernels_agree(cuda_ctx, spheres, mode):
                 np.testing.assert_array_equal(hg.view(np.uint8), outs[0][1].view(np.uint8))
     finally:
         cuda_ctx.set_tuning(**before)
+
+
+def test_noise_octant_4k_sampled_tiles(cuda_ctx):
+    """The noise grid's first octant: product generator (first N5 of its masks), product SDF
+    and pools on the GPU; oracle generator, compute_sdf and atlas() on the CPU."""
+    from test_oracle_workloads import first_n5_slice
+
+    topo = wx.Topology.from_masks(first_n5_slice(W.noise_topology().masks()))
+    assert topo.counts == (1, 443, 367660)
+    grid = cuda_ctx.build_grid(topo)
+    view = orc.workload_view("noise", box=(-2048, 0))
+    frames, ostates = W.noise_frames(), orc.workload_frames("noise")
+    hits = 0
+    for k in (0, 5):
+        rg, hg = sampled_parity(cuda_ctx, grid, view, frames[k], ntiles=800, seed=40 + k, oracle_state=ostates[k][2])
+        f = wx.hit_fields(hg)
+        hits += int((f["state"] == 0).sum())
+        assert (f["level"][f["state"] == 0] == 3).all()
+    assert hits > 10000
 
 
 def test_noise_4k_sampled_tiles(cuda_ctx):

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import woxel_gb300 as wx
-from parity import compare, dispatch_mask, gpu_render, oracle_render
+from parity import compare, dispatch_mask, gpu_render, oracle_render, oracle_view
 
 pytestmark = pytest.mark.gpu
 
@@ -65,7 +65,7 @@ def random_camera(rng, poi):
 def test_fuzz(cuda_ctx, seed):
     rng = np.random.default_rng(1000 + seed)
     topo, vals, poi = random_grid(rng)
-    view = topo.view()
+    view = oracle_view(topo)
     grid = cuda_ctx.build_grid(topo, gpu=bool(rng.integers(2)))
     if vals is not None:
         view["values"], view["band"] = vals

@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 
 import woxel_gb300 as wx
-from parity import compare, dispatch_mask, gpu_render, oracle_render
+from parity import compare, dispatch_mask, gpu_render, oracle_render, oracle_view
 
 pytestmark = pytest.mark.gpu
 
@@ -33,7 +33,7 @@ def test_fast_division_matches_ieee(cuda_ctx, kernel):
 @pytest.fixture(scope="module")
 def sphere64(cuda_ctx):
     topo = wx.Topology.sphere((0, 0, 0), 64.0, 3.0)
-    view = topo.view()
+    view = oracle_view(topo)
     return topo, view, cuda_ctx.build_grid(topo)
 
 
@@ -63,7 +63,7 @@ def test_random_sparse_grids(cuda_ctx, seed):
     rng = np.random.default_rng(seed)
     ijk = rng.integers(-400, 400, size=(3000, 3)).astype(np.int32)
     topo = wx.Topology.from_voxels(ijk)
-    view = topo.view()
+    view = oracle_view(topo)
     grid = cuda_ctx.build_grid(topo)
     eye = tuple(float(x) for x in rng.uniform(-700, 700, 3))
     for mode in (0, 3):
@@ -121,7 +121,7 @@ def test_root_table_and_root_scan(cuda_ctx):
              ((10.0, -20.0, 30.0), (1500, 1500, 1500), 3)]     # eye in key (0,-1,0): no N5 there
     for ijk in (near, np.concatenate([near, far])):
         topo = wx.Topology.from_voxels(ijk.astype(np.int32))
-        view = topo.view()
+        view = oracle_view(topo)
         grid = cuda_ctx.build_grid(topo)
         for eye, target, mode in views:
             st = wx.state_build(eye=eye, target=target, aspect=1.0, fovy=3.0, width=96.0, mode=mode)

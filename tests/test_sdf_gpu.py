@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import woxel_gb300 as wx
-from parity import compare, gpu_render, oracle_render
+from parity import compare, gpu_render, oracle_render, oracle_view
 from woxel_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -54,7 +54,7 @@ def test_sphere_renders_identically(cuda_ctx):
     _, g_gpu, _ = assert_same_pools(cuda_ctx, topo, "sphere64")
     st = wx.state_build(eye=(0, 0, 200), target=(0, 0, 0), aspect=4 / 3, fovy=60.0, width=160.0, mode=3)
     rg, hg = gpu_render(cuda_ctx, g_gpu, st, 160, 120)
-    ro, ho = oracle_render(topo.view(), st, 160, 120)
+    ro, ho = oracle_render(oracle_view(topo), st, 160, 120)
     compare(rg, hg, ro, ho, label="gpu-sdf sphere")
 
 

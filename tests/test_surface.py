@@ -8,11 +8,9 @@ import woxel_gb300 as wx
 
 
 def sphere_view():
-    topo = wx.Topology.sphere((0, 0, 0), 64.0, 3.0)
-    view = topo.view()
-    view["values"] = topo.sphere_values((0, 0, 0), 64.0, 3.0)
-    view["band"] = 3.0
-    return topo, view
+    """The r=64 sphere as the oracle builds it alone: its generator, compute_sdf, atlas()
+    and level-set values."""
+    return wx.Topology.sphere((0, 0, 0), 64.0, 3.0), orc.workload_view("sphere", values=True)
 
 
 def test_values_agree_with_activity():
@@ -52,8 +50,7 @@ def test_crossing_matches_the_analytic_sphere():
 
 
 def test_without_values_no_crossing_is_found():
-    topo = wx.Topology.sphere((0, 0, 0), 64.0, 3.0)
-    view = topo.view()
+    view = orc.workload_view("sphere")
     st = wx.state_build(eye=(0, 0, 200), target=(0, 0, 0), aspect=1.0, fovy=40.0, width=64.0, mode=5)
     rgba, hits, _ = orc.render(view, wx.state_bytes(st), 64, 64, nthreads=4, hits=True)
     assert ((hits["shadow"] & 1) == 0).all()

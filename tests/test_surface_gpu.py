@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 import woxel_gb300 as wx
-from parity import compare, gpu_render, oracle_render
+from parity import compare, gpu_render, oracle_render, oracle_view
 from woxel_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -20,11 +20,14 @@ def compare_surface(rg, hg, ro, ho, label, where=None):
 
 @pytest.fixture(scope="module")
 def sphere_surface(cuda_ctx):
+    """The r=64 sphere: the oracle's view and values built by the oracle alone; the GPU grid
+    and values by the product."""
+    import oracle as orc
+
     topo = wx.Topology.sphere((0, 0, 0), 64.0, 3.0)
-    view = topo.view()
-    view["values"], view["band"] = W.sphere_values(topo), 3.0
+    view = orc.workload_view("sphere", values=True)
     grid = cuda_ctx.build_grid(topo)
-    grid.set_values(view["values"], 3.0)
+    grid.set_values(W.sphere_values(topo), 3.0)
     return view, grid
 
 
@@ -46,7 +49,7 @@ def test_sphere_surface_matches_oracle(cuda_ctx, sphere_surface, kernel):
 
 def test_grid_without_values(cuda_ctx):
     topo = wx.Topology.sphere((0, 0, 0), 64.0, 3.0)
-    view = topo.view()
+    view = oracle_view(topo)
     grid = cuda_ctx.build_grid(topo)
     st = wx.state_build(eye=(0, 0, 200), target=(0, 0, 0), aspect=1.0, fovy=40.0, width=64.0, mode=5)
     rg, hg = gpu_render(cuda_ctx, grid, st, 64, 64)
@@ -55,22 +58,26 @@ def test_grid_without_values(cuda_ctx):
     assert np.isnan(hg["reserved"].view(np.float32)).all()
 
 
-def test_spheres_1080p_surface_sampled_tiles(cuda_ctx):
-    """The 2000-sphere grid with its level-set values, 1080p, 800 random tiles per frame."""
+def test_spheres_1080p_surface_sampled_tiles(cuda_ctx, oracle_spheres_view):
+    """The 2000-sphere grid with its level-set values, 1080p, 800 random tiles per frame. The
+    oracle's view, values and uniforms are its own (restated generators, compute_sdf,
+    atlas(), ComputeState::build); the GPU's are the product's."""
     import oracle as orc
 
     topo = W.spheres_topology()
-    view = topo.view()
-    view["values"], view["band"] = W.spheres_values(topo), 3.0
+    view = oracle_spheres_view
     grid = cuda_ctx.build_grid(topo)
-    grid.set_values(view["values"], 3.0)
-    for k, f in enumerate(W.spheres_frames()[:2]):
+    grid.set_values(W.spheres_values(topo), 3.0)
+    for k, (f, (_, _, osb)) in enumerate(zip(W.spheres_frames()[:2], orc.workload_frames("spheres")[:2])):
         st = f.state()
         st.render_mode[0] = 5
+        ob = bytearray(osb)
+        ob[192:196] = (5).to_bytes(4, "little")  # render_mode, after two matrices and four vec4s
+        assert bytes(ob) == wx.state_bytes(st)
         rg, hg = gpu_render(cuda_ctx, grid, st, f.width, f.height)
         rng = np.random.default_rng(k)
         tiles = np.sort(rng.choice((f.width // 8) * (f.height // 4), 800, replace=False)).astype(np.uint64)
-        ro, ho, _ = orc.render(view, wx.state_bytes(st), f.width, f.height, nthreads=16, hits=True, tiles=tiles)
+        ro, ho, _ = orc.render(view, bytes(ob), f.width, f.height, nthreads=16, hits=True, tiles=tiles)
         m = np.zeros((f.height, f.width), bool)
         for t in tiles:
             x0, y0 = (int(t) % (f.width // 8)) * 8, (int(t) // (f.width // 8)) * 4
@@ -90,7 +97,7 @@ def test_fixture_level_sets(cuda_ctx, name):
     vd = np.load(golden / f"{name}_values.npz")
     vals, bg = vd["values"].astype(np.float32), float(vd["background"])
     topo = wx.Topology.from_masks(m)
-    view = topo.view()
+    view = oracle_view(topo)
     view["values"], view["band"] = vals, bg
     grid = cuda_ctx.build_grid(topo, gpu=True)
     grid.set_values(vals, bg)
