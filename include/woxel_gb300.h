@@ -236,15 +236,18 @@ int wx_batch_destroy(wx_batch *batch);
  * memory until the process exits. The caller passes the grids and the device
  * output buffers.
  * Limits: at most WX_NOALLOC_MAX_FRAMES frames per call (more is rejected with
- * WX_ERR_INVALID); all grids on one device; outputs in device memory; default
- * launch shape (8x4 tiles).
+ * WX_ERR_INVALID); all grids on one device, and `stream` a stream of that
+ * device (else WX_ERR_INVALID); outputs in device memory; default launch shape
+ * (8x4 tiles).
  * The first call on a device does a one-time set-up on that device (it looks
  * up the array's device address and loads the kernels' division table): make
- * that first call before any stream capture. Every call reuses the same array
- * and clears its counter, so calls that overlap on the GPU (on different
- * streams, or from other host threads before earlier work finished) race; the
- * caller must serialise them. The call blocks until earlier work on `stream`
- * is done, because the frame table is copied from pageable host memory. */
+ * that first call before any stream capture. The frame table reaches the array
+ * through the parameters of small table-writing kernels, which the runtime
+ * copies when they are enqueued, so the call does not wait for the GPU and a
+ * later call cannot change the table of an earlier one. Every call reuses the
+ * same array and clears its counter, so calls that overlap on the GPU (on
+ * different streams, or from other host threads before earlier work finished)
+ * race; the caller must serialise them (calls on one stream are ordered). */
 #define WX_NOALLOC_MAX_FRAMES 256
 #define WX_NOALLOC_SCRATCH_BYTES 96512 /* 256 + 256 frames x 376-byte table entries */
 int wx_render_batch_noalloc(const wx_frame *frames, uint32_t n, void *stream);

@@ -74,4 +74,6 @@ def main(assets: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference/assets"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py ASSETS_DIR")
+    main(Path(sys.argv[1]))

@@ -134,3 +134,44 @@ def test_two_streams_and_kernel_switches(cuda_ctx, scene):
     np.testing.assert_array_equal(a[0].cpu().numpy(), refs[-2][0])
     np.testing.assert_array_equal(a[1].cpu().numpy(), refs[-1][0])
     np.testing.assert_array_equal(b.cpu().numpy(), refs[-1][0])
+
+
+def test_two_threads_on_the_per_thread_default_stream(cuda_ctx, scene):
+    """Two host threads, each with its own context, render on cudaStreamPerThread: one handle
+    value that names a different stream in every thread. Each thread writes all frames into
+    one buffer of its own, so every frame must wait for the one before it on its thread's
+    stream; the record of one thread's last frame must never let the other thread's frames skip
+    that wait. Repeated rounds; each buffer ends as the last frame."""
+    import threading
+
+    grid, states, refs = scene
+    per_thread = 2  # cudaStreamPerThread
+    ctxs = [wx.Context(0) for _ in range(2)]
+    for c in ctxs:
+        c.set_tuning(kernel=1, tile_width=4, warps_per_block=4)
+    bufs = [torch.zeros(NPIX * 4, dtype=torch.uint8, device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
+    start = threading.Barrier(2)
+    errors = []
+
+    def work(i):
+        try:
+            start.wait()
+            for _ in range(4):
+                for st in states:
+                    ctxs[i].render(grid, st, 1920, 1080, bufs[i], None, stream=per_thread)
+            torch.cuda.synchronize()
+        except Exception as e:  # reported by the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    torch.cuda.synchronize()
+    for i, b in enumerate(bufs):
+        np.testing.assert_array_equal(b.cpu().numpy(), refs[-1][0], err_msg=f"thread {i}")
+    for c in ctxs:
+        c.close()

@@ -65,3 +65,36 @@ def test_noalloc_rejects_more_than_the_maximum(frames):
     too_many = [(g, st, w, h, r, None)] * (wx.NOALLOC_MAX_FRAMES + 1)
     with pytest.raises(wx.WxError, match="256"):
         wx.render_batch_noalloc(too_many)
+
+
+def test_noalloc_calls_queued_back_to_back(cuda_ctx, frames):
+    """Two calls on one stream with different frames and outputs, the second enqueued before the
+    first has run: each call keeps its own frame table (it travels in the table kernels'
+    launch parameters), so both match the context-based batch."""
+    stream = torch.cuda.current_stream().cuda_stream
+    first, second = frames[:5], frames[3:]
+    expect = []
+    for part in (first, second):
+        ref = buffers(part)
+        cuda_ctx.render_batch([(g, st, w, h, r, hb) for (g, st, w, h), (r, hb) in zip(part, ref)], stream=stream)
+        torch.cuda.synchronize()
+        expect.append(host(ref))
+    got = [buffers(first), buffers(second)]
+    torch.cuda._sleep(20_000_000)  # keep the GPU busy so that both calls are queued before either runs
+    for part, bufs in zip((first, second), got):
+        wx.render_batch_noalloc([(g, st, w, h, r, hb) for (g, st, w, h), (r, hb) in zip(part, bufs)], stream=stream)
+    torch.cuda.synchronize()
+    for p, (exp, bufs) in enumerate(zip(expect, got)):
+        for k, ((e_r, e_h), (g_r, g_h)) in enumerate(zip(exp, host(bufs))):
+            np.testing.assert_array_equal(g_r, e_r, err_msg=f"call {p} frame {k} rgba")
+            np.testing.assert_array_equal(g_h, e_h, err_msg=f"call {p} frame {k} hits")
+
+
+@pytest.mark.skipif(torch.cuda.device_count() < 2, reason="needs a second GPU for a stream of another device")
+def test_noalloc_rejects_a_stream_of_another_device(frames):
+    g, st, w, h = frames[0]
+    r = torch.zeros(w * h * 4, dtype=torch.uint8, device="cuda:0")
+    with torch.cuda.device(1):
+        other = torch.cuda.Stream(device=1)
+    with pytest.raises(wx.WxError, match="another device"):
+        wx.render_batch_noalloc([(g, st, w, h, r, None)], stream=other.cuda_stream)

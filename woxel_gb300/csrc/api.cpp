@@ -110,8 +110,16 @@ constexpr size_t kPixelStreams = 256;  // records kept, oldest dropped first
 std::mutex g_pixel_mu;
 std::vector<PixelOutputs> g_pixel_outputs;
 
-// Records cur as its stream's last k_pixel; true when disjoint from the previous record.
-bool pixel_outputs_disjoint(const PixelOutputs &cur) {
+// Launches k_pixel for cur's outputs and records cur as its stream's last
+// k_pixel, both under g_pixel_mu, so a stream's record always names the k_pixel
+// enqueued on it last even when several host threads launch on one stream. The
+// frame stores without waiting when its outputs are disjoint from the record's.
+// cudaStreamPerThread is one handle for a different stream in every host thread,
+// so no record can name its predecessor: frames on it always wait. NULL and
+// cudaStreamLegacy name the same stream.
+cudaError_t launch_pixel_tracked(const wxk::Job &job, const wxk::Tuning &t, PixelOutputs cur) {
+    if (cur.stream == cudaStreamPerThread) return wxk::launch_pixel(job, t, false, cur.stream);
+    if (cur.stream == cudaStreamLegacy) cur.stream = nullptr;
     auto meet = [](uintptr_t a0, uintptr_t a1, uintptr_t b0, uintptr_t b1) {
         return a0 < a1 && b0 < b1 && a0 < b1 && b0 < a1;
     };
@@ -129,19 +137,9 @@ bool pixel_outputs_disjoint(const PixelOutputs &cur) {
     } else if (v.size() >= kPixelStreams) {
         v.erase(v.begin());
     }
-    v.push_back(cur);
-    return disjoint;
-}
-
-// After a failed launch the stream's last kernel is unknown.
-void forget_pixel_outputs(int device, cudaStream_t st) {
-    std::lock_guard<std::mutex> lock(g_pixel_mu);
-    auto &v = g_pixel_outputs;
-    for (size_t i = 0; i < v.size(); i++)
-        if (v[i].device == device && v[i].stream == st) {
-            v.erase(v.begin() + (long)i);
-            return;
-        }
+    const cudaError_t e = wxk::launch_pixel(job, t, disjoint, cur.stream);
+    if (e == cudaSuccess) v.push_back(cur);  // after a failed launch the stream's last kernel is unknown
+    return e;
 }
 
 bool device_accessible(const void *p) {
@@ -950,12 +948,8 @@ int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, u
             cur.lo[1] = reinterpret_cast<uintptr_t>(out_hits);
             cur.hi[1] = cur.lo[1] + npix * sizeof(wx_hit);
         }
-        const bool disjoint = pixel_outputs_disjoint(cur);
-        const cudaError_t e = wxk::launch_pixel(job, ctx->tuning, disjoint, st);
-        if (e != cudaSuccess) {
-            forget_pixel_outputs(ctx->device, st);
-            return cuda_fail(ctx, e, "wxk::launch_pixel");
-        }
+        const cudaError_t e = launch_pixel_tracked(job, ctx->tuning, cur);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "wxk::launch_pixel");
     } else {
         WX_CUDA(ctx, wxk::launch_persistent(job, ctx->take_counter(), ctx->tuning, ctx->num_sms, st));
     }

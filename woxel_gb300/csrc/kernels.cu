@@ -315,6 +315,26 @@ static_assert(kNoallocBytes == WX_NOALLOC_SCRATCH_BYTES, "scratch size stated in
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
+// The frame table travels to the array as the by-value parameter of a small
+// table-writing kernel (up to kTableChunk frames per launch; launch parameters may
+// take up to 32,764 bytes): the runtime copies a launch's parameters when the
+// launch is enqueued, so a call's table is fixed when the call returns and later
+// calls cannot change what an earlier one reads.
+constexpr uint32_t kTableChunk = (32000 - 8) / sizeof(Job);
+struct TableChunk {
+    uint32_t first, count;  // first table entry written, entries in this chunk
+    Job jobs[kTableChunk];
+};
+static_assert(sizeof(TableChunk) <= 32764, "kernel parameter limit");
+static_assert(sizeof(Job) % 4 == 0, "the table is copied in 4-byte words");
+
+__global__ void k_noalloc_table(const __grid_constant__ TableChunk c) {
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(c.jobs);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(g_noalloc_scratch + kNoallocJobsOffset + (size_t)c.first * sizeof(Job));
+    const uint32_t words = c.count * (uint32_t)(sizeof(Job) / 4);
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+}
+
 // Per-device state of the one-time set-up (host side).
 struct NoallocDevice {
     bool ready = false;
@@ -322,9 +342,8 @@ struct NoallocDevice {
     int num_sms = 0;
 };
 constexpr int kNoallocMaxDevices = 64;
-std::mutex g_noalloc_mu;                     // guards the set-up and the host frame table
+std::mutex g_noalloc_mu;  // guards the one-time set-up
 NoallocDevice g_noalloc_dev[kNoallocMaxDevices];
-Job g_noalloc_table[WX_NOALLOC_MAX_FRAMES];  // host staging of the frame table (static, not heap)
 
 int noalloc_fail(int code, const char *msg) {
     wx::set_thread_error(msg);
@@ -334,6 +353,7 @@ int noalloc_fail(int code, const char *msg) {
 // Once per device, with that device current: find the array's device address
 // (host code cannot use the symbol itself) and load the division table.
 int noalloc_setup(int device, NoallocDevice **out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
     NoallocDevice &d = g_noalloc_dev[device];
     if (!d.ready) {
         cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void **>(&d.scratch), g_noalloc_scratch);
@@ -357,55 +377,83 @@ bool noalloc_device_memory(const void *p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// The table entry of one frame with the default launch shape (8x4 tiles), as
+// wx_render_batch builds it; tiles = queue tiles of the frames before it.
+int noalloc_job(const wx_frame &f, int device, uint64_t tiles, Job &j) {
+    const wxk::Tuning tuning;
+    memset(&j, 0, sizeof j);
+    int gdev = -1;
+    if (!f.rgba8 || !wxk::grid_device_view(f.grid, &j.g, &gdev))
+        return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: frame with a NULL grid or rgba8");
+    if (gdev != device) return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: grids on different devices");
+    if (((uintptr_t)f.rgba8 & 3) || ((uintptr_t)f.hits & 15))
+        return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: rgba8 must be 4-byte and hits 16-byte aligned");
+    if (!noalloc_device_memory(f.rgba8) || (f.hits && !noalloc_device_memory(f.hits)))
+        return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: outputs must be device memory");
+    if ((uint64_t)f.width * f.height >= (1ull << 32))
+        return noalloc_fail(WX_ERR_UNSUPPORTED, "wx_render_batch_noalloc: frame too large");
+    j.width = f.width;
+    j.height = f.height;
+    j.tile_w = (uint16_t)tuning.tile_w;
+    j.tile_h = (uint16_t)(32 / tuning.tile_w);
+    j.order = (uint32_t)tuning.order;
+    j.tiles_x = ((f.width & ~7u) + j.tile_w - 1) / j.tile_w;
+    j.tiles = j.tiles_x * (((f.height & ~3u) + j.tile_h - 1) / j.tile_h);
+    j.tile_begin = (uint32_t)tiles;
+    j.rgba = reinterpret_cast<uint32_t *>(f.rgba8);
+    j.hits = f.hits;
+    j.s = f.state;
+    return WX_OK;
+}
+
 int noalloc_render(int device, const wx_frame *frames, uint32_t n, cudaStream_t st) {
+    int sdev = -1;
+    if (cudaStreamGetDevice(st, &sdev) != cudaSuccess) {
+        cudaGetLastError();
+        return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: stream is not a valid stream");
+    }
+    if (sdev != device)
+        return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: stream belongs to another device than the grids");
     NoallocDevice *d = nullptr;
     int rc = noalloc_setup(device, &d);
     if (rc != WX_OK) return rc;
-    // Frame table with the default launch shape (8x4 tiles), as wx_render_batch builds it.
-    const wxk::Tuning tuning;
+    // Pass 1 checks every frame before anything is enqueued; pass 2 writes the table
+    // one chunk (one table-writing launch) at a time. Frames without dispatched
+    // pixels get no entry, which keeps every entry's tile range non-empty.
+    TableChunk chunk;
     uint32_t njobs = 0;
     uint64_t tiles = 0;
+    bool all = false;
     for (uint32_t i = 0; i < n; i++) {
-        const wx_frame &f = frames[i];
-        Job &j = g_noalloc_table[njobs];
-        memset(&j, 0, sizeof j);
-        int gdev = -1;
-        if (!f.rgba8 || !wxk::grid_device_view(f.grid, &j.g, &gdev))
-            return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: frame with a NULL grid or rgba8");
-        if (gdev != device) return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: grids on different devices");
-        if (((uintptr_t)f.rgba8 & 3) || ((uintptr_t)f.hits & 15))
-            return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: rgba8 must be 4-byte and hits 16-byte aligned");
-        if (!noalloc_device_memory(f.rgba8) || (f.hits && !noalloc_device_memory(f.hits)))
-            return noalloc_fail(WX_ERR_INVALID, "wx_render_batch_noalloc: outputs must be device memory");
-        if ((uint64_t)f.width * f.height >= (1ull << 32))
-            return noalloc_fail(WX_ERR_UNSUPPORTED, "wx_render_batch_noalloc: frame too large");
-        j.width = f.width;
-        j.height = f.height;
-        j.tile_w = (uint16_t)tuning.tile_w;
-        j.tile_h = (uint16_t)(32 / tuning.tile_w);
-        j.order = (uint32_t)tuning.order;
-        j.tiles_x = ((f.width & ~7u) + j.tile_w - 1) / j.tile_w;
-        j.tiles = j.tiles_x * (((f.height & ~3u) + j.tile_h - 1) / j.tile_h);
-        j.tile_begin = (uint32_t)tiles;
-        j.rgba = reinterpret_cast<uint32_t *>(f.rgba8);
-        j.hits = f.hits;
-        j.s = f.state;
-        if (j.tiles == 0) continue;  // nothing dispatched; keep job tile ranges non-empty
+        Job &j = chunk.jobs[0];
+        if ((rc = noalloc_job(frames[i], device, tiles, j)) != WX_OK) return rc;
+        if (j.tiles == 0) continue;
         tiles += j.tiles;
+        all = all || wxk::all_modes(j.s);
         njobs++;
         if (tiles >= (1ull << 31)) return noalloc_fail(WX_ERR_UNSUPPORTED, "wx_render_batch_noalloc: too many tiles");
     }
     if (njobs == 0) return WX_OK;
-    unsigned char *scratch = d->scratch;
-    Job *jobs_dev = reinterpret_cast<Job *>(scratch + kNoallocJobsOffset);
-    uint32_t *counter = reinterpret_cast<uint32_t *>(scratch);
-    // Pageable source: the call returns once the table has been consumed, so
-    // the static host table can be reused by the next call.
-    cudaError_t e = cudaMemcpyAsync(jobs_dev, g_noalloc_table, njobs * sizeof(Job), cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: frame table copy failed");
+    chunk.first = 0;
+    chunk.count = 0;
+    tiles = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        Job &j = chunk.jobs[chunk.count];
+        noalloc_job(frames[i], device, tiles, j);
+        if (j.tiles == 0) continue;
+        tiles += j.tiles;
+        if (++chunk.count == kTableChunk || chunk.first + chunk.count == njobs) {
+            k_noalloc_table<<<1, 256, 0, st>>>(chunk);
+            if (cudaGetLastError() != cudaSuccess)
+                return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: frame table launch failed");
+            chunk.first += chunk.count;
+            chunk.count = 0;
+        }
+    }
+    Job *jobs_dev = reinterpret_cast<Job *>(d->scratch + kNoallocJobsOffset);
+    uint32_t *counter = reinterpret_cast<uint32_t *>(d->scratch);
     wxk::Tuning t;  // defaults; launch_batched clears the counter (it keeps the last call's value otherwise)
-    e = wxk::launch_batched(jobs_dev, njobs, (uint32_t)tiles, counter, t, d->num_sms,
-                            wxk::all_modes(g_noalloc_table, njobs), st);
+    const cudaError_t e = wxk::launch_batched(jobs_dev, njobs, (uint32_t)tiles, counter, t, d->num_sms, all, st);
     if (e != cudaSuccess) return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: launch failed");
     return WX_OK;
 }
@@ -428,11 +476,7 @@ extern "C" int wx_render_batch_noalloc(const wx_frame *frames, uint32_t n, void 
     if (cudaGetDevice(&prev) != cudaSuccess) return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: cudaGetDevice failed");
     if (prev != device && cudaSetDevice(device) != cudaSuccess)
         return noalloc_fail(WX_ERR_CUDA, "wx_render_batch_noalloc: cudaSetDevice failed");
-    int rc;
-    {
-        std::lock_guard<std::mutex> lock(g_noalloc_mu);
-        rc = noalloc_render(device, frames, n, static_cast<cudaStream_t>(stream));
-    }
+    const int rc = noalloc_render(device, frames, n, static_cast<cudaStream_t>(stream));
     if (prev != device) cudaSetDevice(prev);
     return rc;
 }
