@@ -444,6 +444,8 @@ def main():
     ap.add_argument("--blocks-per-sm", type=int, default=None)
     ap.add_argument("--tile-order", type=int, default=None, choices=[0, 1],
                     help="0 tile rows top to bottom, 1 middle rows first")
+    ap.add_argument("--rays-per-lane", type=int, default=None, choices=[1, 2, 4, 8],
+                    help="tiles per warp of the per-frame kernel with lanes that refill (1: one pixel per lane)")
     args = ap.parse_args()
     if args.cpu_fraction is None:
         args.cpu_fraction = {"sphere": 1.0, "spheres": 1.0 / 8, "noise": 1.0 / 32}[args.workload]
@@ -477,7 +479,7 @@ def main():
     t_gen = time.perf_counter() - t0
     ctx = wx.Context(local)
     tune = {} if args.kernel is None else {"kernel": 0 if args.kernel == "persistent" else 1}
-    for k in ("tile_width", "warps_per_block", "blocks_per_sm", "tile_order"):
+    for k in ("tile_width", "warps_per_block", "blocks_per_sm", "tile_order", "rays_per_lane"):
         if getattr(args, k) is not None:
             tune[k] = getattr(args, k)
     ctx.set_tuning(**tune)
@@ -510,12 +512,12 @@ def main():
 
     tuned = None
     if (args.autotune and args.kernel is None and args.tile_width is None and args.warps_per_block is None
-            and args.tile_order is None):
+            and args.tile_order is None and args.rays_per_lane is None):
         t0 = time.perf_counter()
         tuned = ctx.autotune([(grid, st, W_, H_, o, None) for st, o in list(zip(states, outs))[:4]], reps=2)
         tuned["seconds"] = time.perf_counter() - t0
         tuned["table"] = [[c["kernel"], c["tile_width"], c["warps_per_block"], c["blocks_per_sm"], c["tile_order"],
-                           round(ms, 4)]
+                           c["rays_per_lane"], round(ms, 4)]
                           for c, ms in tuned["table"]]
         log(f"[bench] autotune -> {tuned['best']} in {tuned['seconds']:.1f}s")
     for _ in range(args.warmup):
@@ -657,7 +659,8 @@ def main():
 
     # roofline + CPU baseline from the oracle on a sample of the same tiles (rank 0)
     roof, cpu, graze = None, None, None
-    kernel_name = "k_persistent" if ctx.tuning["kernel"] == 0 else "k_pixel"  # after autotuning
+    tn = ctx.tuning  # after autotuning
+    kernel_name = "k_persistent" if tn["kernel"] == 0 else ("k_wave" if tn["rays_per_lane"] > 1 else "k_pixel")
     if rank == 0:
         peak, peak_kind = hbm_peak()
         t0 = time.perf_counter()
@@ -708,7 +711,7 @@ def main():
                     "device_bytes": info["device_bytes"],
                     "grid_build_s": {"host_sdf": round(t_build, 3), "gpu_sdf": round(t_build_gpu, 3)},
                     "tuning": ctx.tuning,
-                    "autotune": tuned and {"table [kernel, tile_w, warps/block, blocks/SM (0 = all that fit), tile order (1 = middle rows first), ms for 4 frames]":
+                    "autotune": tuned and {"table [kernel, tile_w, warps/block, blocks/SM (0 = all that fit), tile order (1 = middle rows first), rays per lane, ms for 4 frames]":
                                            tuned["table"],
                                            "seconds": tuned["seconds"]}},
             "frame_latency_ms": {"p50": p50, "p99": p99},

@@ -125,6 +125,12 @@ typedef struct wx_tuning {
                                 above and below it, so that the costly centre of a centred
                                 view starts first and a frame's last tiles are its cheap
                                 edges. The pixels written are the same either way. */
+    int32_t rays_per_lane;   /* kernel 1 only, modes 0-3: 1 (default) one pixel per lane;
+                                2, 4 or 8: each warp takes that many consecutive tiles and a
+                                lane whose ray has ended takes the warp's next pixel, so the
+                                march runs with most lanes busy (results are shaded, and
+                                shadow rays marched, in the same way afterwards). The pixels
+                                written are the same either way. */
 } wx_tuning;
 
 /* One frame of a batched launch: a camera uniform over one resident grid. */
@@ -156,8 +162,17 @@ int wx_grid_build(wx_ctx *ctx, wx_topology *topo, wx_grid **out);
 /* wx_grid_build with the SDF and the packing on the GPU (compute_sdf,
  * vdb345.rs:290-670): the same device pools word for word. Needs N5 origins
  * that are multiples of 4096 (else WX_ERR_UNSUPPORTED). Temporary device
- * memory: about 4 bytes per leaf voxel plus 200 bytes per node. */
+ * memory: about 4 bytes per leaf voxel plus 200 bytes per node.
+ * The sweeps hand containers to CTAs through a ready queue; a CTA whose
+ * container is not ready polls for it, at most the context's SDF wait limit
+ * (wx_ctx_set_sdf_wait_limit) times, then sets an error flag on which every
+ * CTA returns: the call then returns WX_ERR_TIMEOUT, builds no grid and leaves
+ * the context usable. */
 int wx_grid_build_gpu(wx_ctx *ctx, const wx_topology *topo, wx_grid **out);
+/* Bound of wx_grid_build_gpu's waits, in polls 256 ns apart (0 restores the
+ * default, 2^23, about 2 s). No counterpart in the reference, whose failures
+ * panic (wgpu_context.rs:44-101). */
+int wx_ctx_set_sdf_wait_limit(wx_ctx *ctx, uint32_t polls);
 int wx_grid_release(wx_ctx *ctx, wx_grid *grid);
 /* Attaches level-set values for WX_MODE_SURFACE: one float per leaf voxel
  * (n3 * 512, DFS leaf order, voxel order x<<6 | y<<3 | z), the signed distance
@@ -203,10 +218,13 @@ int wx_ctx_get_tuning(const wx_ctx *ctx, wx_tuning *tuning);
 /* Autotuner: renders `frames` (device outputs, as for wx_render_batch) once per
  * frame with each candidate tuning, reps times after one warm-up pass, timing
  * with CUDA events, and installs the fastest on the context. candidates NULL
- * (ncand ignored) uses the built-in set: for tile orders 1 then 0, both kernels
- * x tile widths {4, 8, 16} x {2, 4, 8} warps per block, plus the persistent
- * kernel at 4 blocks of 4 warps per SM (tile widths 4, 8). times_ms (ncand or
- * 40 entries, may be NULL) receives each candidate's mean time for all frames. */
+ * (ncand ignored) uses the built-in set of WX_AUTOTUNE_BUILTIN candidates: for
+ * tile orders 1 then 0, both kernels x tile widths {4, 8, 16} x {2, 4, 8} warps
+ * per block at one ray per lane, the persistent kernel at 4 blocks of 4 warps per
+ * SM (tile widths 4, 8), and kernel 1 with {2, 4, 8} rays per lane x tile widths
+ * {4, 8} x {2, 4} warps per block. times_ms (ncand or WX_AUTOTUNE_BUILTIN
+ * entries, may be NULL) receives each candidate's mean time for all frames. */
+#define WX_AUTOTUNE_BUILTIN 64
 int wx_autotune(wx_ctx *ctx, const wx_frame *frames, uint32_t n, const wx_tuning *candidates, uint32_t ncand,
                 uint32_t reps, wx_tuning *best, double *times_ms);
 

@@ -45,7 +45,7 @@ def test_binding_covers_header():
 def test_struct_sizes():
     assert C.sizeof(wx.wx_state_uniform) == 256
     assert C.sizeof(wx.wx_hit) == 32
-    assert C.sizeof(wx.wx_tuning) == 20
+    assert C.sizeof(wx.wx_tuning) == 24
     assert wx.HIT_DTYPE.itemsize == 32
 
 

@@ -19,8 +19,10 @@ pytestmark = pytest.mark.gpu
 NPIX = 1920 * 1080
 
 
-@pytest.fixture(scope="module")
-def scene(cuda_ctx):
+@pytest.fixture(scope="module", params=[1, 4], ids=["rays1", "rays4"])
+def scene(cuda_ctx, request):
+    """The frames and their references; every test runs with one ray per lane (k_pixel) and with
+    four (lanes that refill)."""
     grid = cuda_ctx.build_grid(W.spheres_topology())
     frames = W.spheres_frames()[:8]
     states = [f.state() for f in frames]
@@ -32,7 +34,7 @@ def scene(cuda_ctx):
         cuda_ctx.render(grid, st, 1920, 1080, o, h)
         torch.cuda.synchronize()
         refs.append((o.cpu().numpy(), h.cpu().numpy()))
-    cuda_ctx.set_tuning(kernel=1, tile_width=4, warps_per_block=4)
+    cuda_ctx.set_tuning(kernel=1, tile_width=4, warps_per_block=4, rays_per_lane=request.param)
     yield grid, states, refs
     cuda_ctx.set_tuning(**before)
 
@@ -102,7 +104,7 @@ def test_colour_of_one_frame_over_hit_records_of_the_last(cuda_ctx, scene):
 def test_two_contexts_on_one_stream(cuda_ctx, scene):
     grid, states, refs = scene
     other = wx.Context(0)
-    other.set_tuning(kernel=1, tile_width=4, warps_per_block=4)
+    other.set_tuning(**cuda_ctx.tuning)
     grid2 = other.build_grid(W.spheres_topology())
     torch.cuda.synchronize()
     buf = torch.zeros(NPIX * 4, dtype=torch.uint8, device="cuda")
@@ -148,7 +150,7 @@ def test_two_threads_on_the_per_thread_default_stream(cuda_ctx, scene):
     per_thread = 2  # cudaStreamPerThread
     ctxs = [wx.Context(0) for _ in range(2)]
     for c in ctxs:
-        c.set_tuning(kernel=1, tile_width=4, warps_per_block=4)
+        c.set_tuning(**cuda_ctx.tuning)
     bufs = [torch.zeros(NPIX * 4, dtype=torch.uint8, device="cuda") for _ in range(2)]
     torch.cuda.synchronize()
     start = threading.Barrier(2)

@@ -82,8 +82,9 @@ def test_spheres_batched_equals_plain_and_repeatable(cuda_ctx, spheres):
 
 @pytest.mark.parametrize("mode", [3, 0])
 def test_spheres_all_kernels_agree(cuda_ctx, spheres, mode):
-    """Whole 1080p frames: the per-tile kernel, other tile shapes and both tile-row orders write
-    the same RGBA8 and hit records as the tile-queue kernel, bit for bit."""
+    """Whole 1080p frames: the per-tile kernel, other tile shapes, both tile-row orders and 2, 4 and 8
+    rays per lane (lanes that refill) write the same RGBA8 and hit records as the tile-queue kernel,
+    bit for bit."""
     _, _, grid = spheres
     before = cuda_ctx.tuning
     try:
@@ -91,8 +92,9 @@ def test_spheres_all_kernels_agree(cuda_ctx, spheres, mode):
             st = f.state()
             st.render_mode[0] = mode
             outs = []
-            for k, tw, order in ((0, 8, 1), (1, 4, 1), (0, 16, 0), (1, 32, 1), (1, 4, 0), (0, 4, 0)):
-                cuda_ctx.set_tuning(kernel=k, tile_width=tw, tile_order=order)
+            for k, tw, order, rays in ((0, 8, 1, 1), (1, 4, 1, 1), (0, 16, 0, 1), (1, 32, 1, 1), (1, 4, 0, 1),
+                                       (0, 4, 0, 1), (1, 4, 1, 4), (1, 8, 0, 2), (1, 4, 1, 8)):
+                cuda_ctx.set_tuning(kernel=k, tile_width=tw, tile_order=order, rays_per_lane=rays)
                 outs.append(gpu_render(cuda_ctx, grid, st, f.width, f.height))
             for rg, hg in outs[1:]:
                 np.testing.assert_array_equal(rg, outs[0][0])

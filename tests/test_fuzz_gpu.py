@@ -11,11 +11,14 @@ from parity import compare, dispatch_mask, gpu_render, oracle_render, oracle_vie
 
 pytestmark = pytest.mark.gpu
 
-TUNINGS = [dict(kernel=0, tile_width=8, warps_per_block=4, blocks_per_sm=0, tile_order=1),
-           dict(kernel=1, tile_width=4, warps_per_block=2, blocks_per_sm=0, tile_order=0),
-           dict(kernel=0, tile_width=16, warps_per_block=8, blocks_per_sm=0, tile_order=0),
-           dict(kernel=1, tile_width=32, warps_per_block=4, blocks_per_sm=0, tile_order=1),
-           dict(kernel=0, tile_width=4, warps_per_block=4, blocks_per_sm=4, tile_order=1)]
+TUNINGS = [dict(kernel=0, tile_width=8, warps_per_block=4, blocks_per_sm=0, tile_order=1, rays_per_lane=1),
+           dict(kernel=1, tile_width=4, warps_per_block=2, blocks_per_sm=0, tile_order=0, rays_per_lane=1),
+           dict(kernel=0, tile_width=16, warps_per_block=8, blocks_per_sm=0, tile_order=0, rays_per_lane=1),
+           dict(kernel=1, tile_width=32, warps_per_block=4, blocks_per_sm=0, tile_order=1, rays_per_lane=1),
+           dict(kernel=0, tile_width=4, warps_per_block=4, blocks_per_sm=4, tile_order=1, rays_per_lane=1),
+           dict(kernel=1, tile_width=8, warps_per_block=4, blocks_per_sm=0, tile_order=1, rays_per_lane=4),
+           dict(kernel=1, tile_width=4, warps_per_block=2, blocks_per_sm=0, tile_order=0, rays_per_lane=8),
+           dict(kernel=1, tile_width=16, warps_per_block=8, blocks_per_sm=0, tile_order=1, rays_per_lane=2)]
 
 
 def random_grid(rng):

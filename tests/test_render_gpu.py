@@ -8,16 +8,19 @@ from parity import compare, dispatch_mask, gpu_render, oracle_render, oracle_vie
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(params=["persistent", "pixel", "pixel-16x2", "persistent-4x8", "persistent-4blocks", "pixel-rows"],
+@pytest.fixture(params=["persistent", "pixel", "pixel-16x2", "persistent-4x8", "persistent-4blocks", "pixel-rows",
+                        "wave4", "wave2-4x8", "wave8-16x2-rows"],
                 autouse=True)
 def kernel(request, cuda_ctx):
-    """Run every parity test on both kernels, on non-default pixel tile shapes, at reduced occupancy
-    and with tile rows handed out top to bottom."""
+    """Run every parity test on both kernels, on non-default pixel tile shapes, at reduced occupancy,
+    with tile rows handed out top to bottom, and with 2, 4 and 8 rays per lane (lanes that refill)."""
     before = cuda_ctx.tuning
-    tw = {"pixel-16x2": 16, "persistent-4x8": 4}.get(request.param, 8)
-    bps = 4 if request.param == "persistent-4blocks" else 0
-    cuda_ctx.set_tuning(kernel=0 if request.param.startswith("persistent") else 1, tile_width=tw,
-                        blocks_per_sm=bps, warps_per_block=4, tile_order=0 if request.param == "pixel-rows" else 1)
+    p = request.param
+    tw = {"pixel-16x2": 16, "persistent-4x8": 4, "wave2-4x8": 4, "wave8-16x2-rows": 16}.get(p, 8)
+    bps = 4 if p == "persistent-4blocks" else 0
+    rays = {"wave4": 4, "wave2-4x8": 2, "wave8-16x2-rows": 8}.get(p, 1)
+    cuda_ctx.set_tuning(kernel=0 if p.startswith("persistent") else 1, tile_width=tw, blocks_per_sm=bps,
+                        warps_per_block=4, tile_order=0 if p.endswith("rows") else 1, rays_per_lane=rays)
     yield request.param
     cuda_ctx.set_tuning(**before)
 

@@ -330,6 +330,10 @@ class Context:
         t = wx_tuning(**cur)
         check(lib().wx_ctx_set_tuning(self._h, C.byref(t)), self._h)
 
+    def set_sdf_wait_limit(self, polls: int) -> None:
+        """Bound of the GPU SDF build's dependency waits (polls 256 ns apart; 0 = default, about 2 s)."""
+        check(lib().wx_ctx_set_sdf_wait_limit(self._h, polls), self._h)
+
     def autotune(self, frames: Sequence, candidates: Optional[Sequence[dict]] = None, reps: int = 3) -> dict:
         """Time candidate launch shapes on `frames` ((grid, state, w, h, rgba_dev, hits_dev) tuples) and
         install the fastest. Returns {"best": tuning, "table": [(tuning, ms), ...]}."""
@@ -337,9 +341,12 @@ class Context:
         if candidates is None:
             cands = []
             for o in (1, 0):  # the built-in set of wx_autotune, in its order
-                cands += [dict(kernel=k, warps_per_block=w, blocks_per_sm=0, tile_width=t, tile_order=o)
+                cands += [dict(kernel=k, warps_per_block=w, blocks_per_sm=0, tile_width=t, tile_order=o, rays_per_lane=1)
                           for k in (0, 1) for t in (4, 8, 16) for w in (2, 4, 8)]
-                cands += [dict(kernel=0, warps_per_block=4, blocks_per_sm=4, tile_width=t, tile_order=o) for t in (4, 8)]
+                cands += [dict(kernel=0, warps_per_block=4, blocks_per_sm=4, tile_width=t, tile_order=o,
+                               rays_per_lane=1) for t in (4, 8)]
+                cands += [dict(kernel=1, warps_per_block=w, blocks_per_sm=0, tile_width=t, tile_order=o,
+                               rays_per_lane=r) for r in (2, 4, 8) for t in (4, 8) for w in (2, 4)]
         else:
             cands = [dict(self.tuning, **c) for c in candidates]
         carr = (wx_tuning * len(cands))(*[wx_tuning(**c) for c in cands])

@@ -40,7 +40,7 @@ class wx_grid_info(C.Structure):
 
 class wx_tuning(C.Structure):
     _fields_ = [("kernel", C.c_int32), ("warps_per_block", C.c_int32), ("blocks_per_sm", C.c_int32),
-                ("tile_width", C.c_int32), ("tile_order", C.c_int32)]
+                ("tile_width", C.c_int32), ("tile_order", C.c_int32), ("rays_per_lane", C.c_int32)]
 
 
 class wx_frame(C.Structure):
@@ -100,6 +100,7 @@ SIGNATURES = {
     "wx_render": (INT, [P, P, C.POINTER(wx_state_uniform), U32, U32, P, P, P]),
     "wx_ctx_set_tuning": (INT, [P, C.POINTER(wx_tuning)]),
     "wx_ctx_get_tuning": (INT, [P, C.POINTER(wx_tuning)]),
+    "wx_ctx_set_sdf_wait_limit": (INT, [P, C.c_uint32]),
     "wx_render_batch": (INT, [P, C.POINTER(wx_frame), U32, P]),
     "wx_batch_create": (INT, [P, C.POINTER(wx_frame), U32, C.POINTER(P)]),
     "wx_batch_launch": (INT, [P, P]),

@@ -51,6 +51,7 @@ struct wx_ctx {
     size_t jobs_cap = 0;
     wxk::Job *jobs_host = nullptr;      // pinned staging for that table
     cudaEvent_t jobs_done = nullptr;    // last one-shot batch's table copy
+    uint32_t sdf_spins = wxk::kSdfSpinLimit;  // bound of the GPU SDF sweeps' dependency waits
     uint32_t *take_counter() {
         uint32_t *c = counters + next_counter;
         next_counter = (next_counter + 1) % kCounterSlots;
@@ -450,13 +451,21 @@ int wx_ctx_set_tuning(wx_ctx *ctx, const wx_tuning *t) {
     if (!ctx || !t) return fail(ctx, WX_ERR_INVALID, "wx_ctx_set_tuning: null argument");
     const bool tw_ok = t->tile_width == 4 || t->tile_width == 8 || t->tile_width == 16 || t->tile_width == 32;
     if (t->kernel < 0 || t->kernel > 1 || t->warps_per_block < 1 || t->warps_per_block > 8 || t->blocks_per_sm < 0 ||
-        t->blocks_per_sm > 64 || !tw_ok || t->tile_order < 0 || t->tile_order > 1)
+        t->blocks_per_sm > 64 || !tw_ok || t->tile_order < 0 || t->tile_order > 1 ||
+        !(t->rays_per_lane == 1 || t->rays_per_lane == 2 || t->rays_per_lane == 4 || t->rays_per_lane == 8))
         return fail(ctx, WX_ERR_INVALID, "wx_ctx_set_tuning: value out of range");
     ctx->tuning.kernel = t->kernel;
     ctx->tuning.warps_per_block = t->warps_per_block;
     ctx->tuning.blocks_per_sm = t->blocks_per_sm;
     ctx->tuning.tile_w = t->tile_width;
     ctx->tuning.order = t->tile_order;
+    ctx->tuning.rays = t->rays_per_lane;
+    return WX_OK;
+}
+
+int wx_ctx_set_sdf_wait_limit(wx_ctx *ctx, uint32_t polls) {
+    if (!ctx) return WX_ERR_INVALID;
+    ctx->sdf_spins = polls ? polls : wxk::kSdfSpinLimit;
     return WX_OK;
 }
 
@@ -467,6 +476,7 @@ int wx_ctx_get_tuning(const wx_ctx *ctx, wx_tuning *t) {
     t->blocks_per_sm = ctx->tuning.blocks_per_sm;
     t->tile_width = ctx->tuning.tile_w;
     t->tile_order = ctx->tuning.order;
+    t->rays_per_lane = ctx->tuning.rays;
     return WX_OK;
 }
 
@@ -481,10 +491,15 @@ int wx_autotune(wx_ctx *ctx, const wx_frame *frames, uint32_t n, const wx_tuning
         for (int order : {1, 0}) {
             for (int kernel : {0, 1})
                 for (int tw : {4, 8, 16})
-                    for (int wpb : {2, 4, 8}) cand.push_back(wx_tuning{kernel, wpb, 0, tw, order});
+                    for (int wpb : {2, 4, 8}) cand.push_back(wx_tuning{kernel, wpb, 0, tw, order, 1});
             // Occupancy of the persistent kernel: fewer resident warps than fit (16 per SM).
-            for (int tw : {4, 8}) cand.push_back(wx_tuning{0, 4, 4, tw, order});
+            for (int tw : {4, 8}) cand.push_back(wx_tuning{0, 4, 4, tw, order, 1});
+            // Rays per lane: warps of several tiles whose lanes refill.
+            for (int rays : {2, 4, 8})
+                for (int tw : {4, 8})
+                    for (int wpb : {2, 4}) cand.push_back(wx_tuning{1, wpb, 0, tw, order, rays});
         }
+        if (cand.size() != WX_AUTOTUNE_BUILTIN) return fail(ctx, WX_ERR_INVALID, "wx_autotune: built-in set size");
     }
     if (cand.empty()) return fail(ctx, WX_ERR_INVALID, "wx_autotune: no candidates");
     for (uint32_t i = 0; i < n; i++)
@@ -708,14 +723,15 @@ int wx_grid_build_gpu(wx_ctx *ctx, const wx_topology *t, wx_grid **out) {
     for (auto &lv : levels) {
         WX_CUDA(ctx, wxk::sdf_neighbours(lv.L, lv.org->as<int4>(), (uint32_t)lv.nc, tree, nb.as<uint32_t>(), st));
         WX_CUDA(ctx, wxk::sdf_sweep(lv.L, lv.d->as<uint32_t>(), nb.as<uint32_t>(), (uint32_t)lv.nc,
-                                    indeg.as<uint32_t>(), queue.as<uint32_t>(), ctr.as<uint32_t>(), ctx->num_sms, st));
+                                    indeg.as<uint32_t>(), queue.as<uint32_t>(), ctr.as<uint32_t>(), ctx->num_sms,
+                                    ctx->sdf_spins, st));
     }
     // Count the leaf overflow entries (ctr[3]) to size the grid block.
     uint32_t *flags = ctr.as<uint32_t>();
     WX_CUDA(ctx, wxk::sdf_pack_leaves(d3.as<uint32_t>(), n3 * kN3Slots, nullptr, nullptr, 0, flags + 3, st));
     uint32_t h[8];
     WX_CUDA(ctx, cudaMemcpy(h, flags, sizeof h, cudaMemcpyDeviceToHost));
-    if (h[2]) return fail(ctx, WX_ERR_CUDA, "wx_grid_build_gpu: a sweep's dependency wait hit its bound");
+    if (h[2]) return fail(ctx, WX_ERR_TIMEOUT, "wx_grid_build_gpu: a sweep's dependency wait hit its bound");
     const uint64_t n_ovf = h[3];
     wx_grid *gr = nullptr;
     if ((rc = alloc_grid(ctx, o5, n5, n4, n3, n_ovf, &gr)) != WX_OK) return rc;

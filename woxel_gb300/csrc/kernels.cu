@@ -30,21 +30,27 @@ using wxk::Job;
 // (wgpu_context.rs:281) do nothing. kAll = false compiles modes 0-3 only (the
 // host sends frames of modes 4 and 5 to the kAll = true kernels): the glossy
 // chain and the zero-crossing search would otherwise cost the march registers.
-template <bool kAll>
-__device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t lane, bool wait_prev) {
-    // Tile row: with order 1, the i-th row handed out is the middle row, then
-    // alternately the rows above and below it (a permutation of the rows).
+// Pixel (gx, gy) of lane `lane` of tile tl; false outside the dispatched region.
+// Tile row: with order 1, the i-th row handed out is the middle row, then
+// alternately the rows above and below it (a permutation of the rows).
+__device__ __forceinline__ bool tile_pixel(const Job &J, uint32_t tl, uint32_t lane, uint32_t &gx, uint32_t &gy) {
     uint32_t row = tl / J.tiles_x;
     if (J.order) {
         const uint32_t mid = (J.tiles / J.tiles_x) >> 1;
         row = (row & 1u) ? mid - ((row + 1u) >> 1) : mid + (row >> 1);
     }
-    const uint32_t gx = (tl % J.tiles_x) * J.tile_w + lane % J.tile_w;
-    const uint32_t gy = row * J.tile_h + lane / J.tile_w;
+    gx = (tl % J.tiles_x) * J.tile_w + lane % J.tile_w;
+    gy = row * J.tile_h + lane / J.tile_w;
+    return gx < (J.width & ~7u) && gy < (J.height & ~3u);
+}
+
+template <bool kAll>
+__device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t lane, bool wait_prev) {
+    uint32_t gx, gy;
     // The warp's lanes leave each march at different iterations. Without the
     // explicit reconvergence points below they go on in small groups, each
     // running the shading once and starting its own shadow march.
-    const bool valid = gx < (J.width & ~7u) && gy < (J.height & ~3u);
+    const bool valid = tile_pixel(J, tl, lane, gx, gy);
     const uint32_t act = __ballot_sync(~0u, valid);
     if (!valid) return;
     const wx_state_uniform &s = J.s;
@@ -129,6 +135,212 @@ __global__ void WX_PIXEL_BOUNDS k_pixel(const __grid_constant__ Job job, uint32_
     render_pixel<kAll>(job, tile, threadIdx.x & 31u, disjoint == 0u);
 }
 
+// ---------------------------------------------------------------------------
+// k_wave: lanes that refill (modes 0-3). One warp per work unit of kR
+// consecutive tiles (kR * 32 pixels, kR rays per lane on average). A lane whose
+// ray has ended takes the unit's next pixel as soon as kRefill lanes of the
+// warp are idle, so the march runs with most lanes busy; the ray's result goes
+// to the warp's shared-memory slots and the unit's pixels are shaded 32 at a
+// time once every ray has ended. The unit's shadow rays (mode 3) are queued in
+// the same slots and marched the same way. Every ray performs exactly the
+// ray_step sequence it performs in k_pixel, so pixels and hit records are
+// identical. Launched like k_pixel (programmatic dependent launch).
+// ---------------------------------------------------------------------------
+constexpr uint32_t kWaveWords = 5;               // slot: p.xyz, info, node | queued shadow ray: src.xyz, pixel, colour
+constexpr uint32_t kSlotInvalid = 0xFFFFFFFFu;   // info of a pixel outside the dispatched region
+constexpr uint32_t kSlotDeferred = 0xFFFFFFFEu;  // info of a ray for the careful step, marched after the others
+constexpr uint32_t kRefill = 8;                  // idle lanes that trigger a refill
+
+__device__ __forceinline__ void wave_put(uint32_t *q, const Ray &r, uint32_t st) {
+    q[0] = __float_as_uint(r.px);
+    q[1] = __float_as_uint(r.py);
+    q[2] = __float_as_uint(r.pz);
+    q[3] = st | (r.np << 2) | (ray_mask(r) << 4) | (r.i << 8);
+    q[4] = ray_node(r);
+}
+
+// The shadow record of a traced shadow ray and the pixel's colour: I_a when the
+// shadow ray hit, else the queued I_a + I_d (raycast.comp.wgsl:188-193).
+__device__ __forceinline__ void wave_shadow_done(const Job &J, const uint32_t *e, uint32_t ambient, uint32_t st,
+                                                 uint32_t steps) {
+    const uint32_t pixel = e[3];
+    if (!wx_in_range(pixel, (uint64_t)J.width * J.height)) return;
+    J.rgba[pixel] = st == 0u ? ambient : e[4] | 0xFF000000u;
+    if (J.hits) reinterpret_cast<uint32_t *>(J.hits + pixel)[6] = 1u | (st << 1) | (steps << 8);
+}
+
+#define WX_WAVE_BOUNDS __launch_bounds__(256, 5)
+
+template <uint32_t kR>
+__global__ void WX_WAVE_BOUNDS k_wave(const __grid_constant__ Job J, uint32_t ntiles, uint32_t disjoint) {
+    extern __shared__ uint32_t wave_smem[];
+    if (blockIdx.x == 0) asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;");
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t tile0 = (blockIdx.x * (blockDim.x >> 5) + warp) * kR;
+    if (tile0 >= ntiles) return;
+    const uint32_t P = min(kR, ntiles - tile0) * 32u;  // the unit's pixels
+    uint32_t *slot = wave_smem + warp * (kR * 32u * kWaveWords);
+    const wx_state_uniform &s = J.s;
+    const F3 eye = f3(s.eye[0], s.eye[1], s.eye[2]);
+    const uint32_t below = (1u << lane) - 1u;
+
+    // Phase 1: primary rays, lanes refilled from the unit's pixels.
+    {
+        Ray r;
+        bool active = false;
+        uint32_t mine = 0, next = 0;
+        for (;;) {
+            const uint32_t idle = __ballot_sync(~0u, !active);
+            if (next < P && (idle == ~0u || __popc(idle) >= kRefill)) {
+                if (!active) {
+                    const uint32_t pix = next + __popc(idle & below);
+                    if (pix < P) {
+                        uint32_t gx, gy;
+                        if (!tile_pixel(J, tile0 + pix / 32u, pix % 32u, gx, gy)) {
+                            slot[pix * kWaveWords + 3] = kSlotInvalid;
+                        } else {
+                            const F3 dir = primary_dir(s, gx, gy);
+                            if (ray_needs_careful_step(eye, dir)) {
+                                slot[pix * kWaveWords + 3] = kSlotDeferred;
+                            } else {
+                                ray_init(r, eye, dir);
+                                active = true;
+                                mine = pix;
+                            }
+                        }
+                    }
+                }
+                next += __popc(idle);
+                continue;
+            }
+            if (idle == ~0u) break;
+            if (active) {
+                const uint32_t st = ray_step<false>(J.g, r);
+                if (st != 0xFFu) {
+                    wave_put(slot + mine * kWaveWords, r, st);
+                    active = false;
+                }
+            }
+        }
+    }
+    __syncwarp();
+    // Rays that need the careful step (a direction component below 2^-126 in
+    // magnitude, or a -0 eye coordinate): rare, marched 32 at a time.
+    for (uint32_t base = 0; base < P; base += 32u) {
+        const uint32_t pix = base + lane;
+        const bool mine = slot[pix * kWaveWords + 3] == kSlotDeferred;
+        if (!__any_sync(~0u, mine)) continue;
+        if (mine) {
+            uint32_t gx, gy;
+            tile_pixel(J, tile0 + pix / 32u, lane, gx, gy);
+            Ray r;
+            ray_init(r, eye, primary_dir(s, gx, gy));
+            uint32_t st;
+            while ((st = ray_step<true>(J.g, r)) == 0xFFu) {
+            }
+            wave_put(slot + pix * kWaveWords, r, st);
+        }
+        __syncwarp();
+    }
+
+    // Phase 2: shading, 32 pixels at a time; lit pixels of mode 3 queue their
+    // shadow ray in the slots already read.
+    const bool wait_prev = disjoint == 0u;
+    uint32_t nq = 0;
+    for (uint32_t base = 0; base < P; base += 32u) {
+        const uint32_t pix = base + lane;
+        const uint32_t *q = slot + pix * kWaveWords;
+        March hit;
+        hit.p = f3(__uint_as_float(q[0]), __uint_as_float(q[1]), __uint_as_float(q[2]));
+        const uint32_t info = q[3];
+        hit.node = q[4];
+        const bool valid = info != kSlotInvalid;
+        hit.state = info & 3u;
+        hit.np = (info >> 2) & 3u;
+        hit.mask = (info >> 4) & 7u;
+        hit.i = info >> 8;
+        uint32_t gx, gy;
+        tile_pixel(J, tile0 + pix / 32u, lane, gx, gy);
+        const F3 dir = primary_dir(s, gx, gy);
+        bool need = false;
+        F3 shadowed, src;
+        const F3 c = primary_colour(s, hit, dir, &need, &shadowed, &src);
+        need = need && valid;
+        __syncwarp();  // every slot of these 32 pixels is read before the queue reuses them
+        const uint32_t qm = __ballot_sync(~0u, need);
+        const uint32_t pixel = gy * J.width + gx;
+        if (need) {
+            uint32_t *e = slot + (nq + __popc(qm & below)) * kWaveWords;
+            e[0] = __float_as_uint(src.x);
+            e[1] = __float_as_uint(src.y);
+            e[2] = __float_as_uint(src.z);
+            e[3] = pixel;
+            e[4] = pack_rgba(c);
+        }
+        nq += __popc(qm);
+        if (valid) {
+            if (wait_prev) asm volatile("griddepcontrol.wait;" ::: "memory");
+            if (wx_in_range(pixel, (uint64_t)J.width * J.height)) {
+                if (!need) J.rgba[pixel] = pack_rgba(c);
+                if (J.hits) store_hit(J.hits + pixel, hit.p, dot3(hit.p - eye, dir), hit.node, info, 0u);
+            }
+        }
+    }
+    if (nq == 0u) return;
+    __syncwarp();
+
+    // Phase 3: the queued shadow rays toward the sun, lanes refilled from the queue.
+    const F3 sdir = -f3(s.sun_dir[0], s.sun_dir[1], s.sun_dir[2]);
+    const uint32_t ambient = pack_rgba(ambient_colour());
+    const bool dir_careful = !(fabsf(sdir.x) >= 0x1p-126f && fabsf(sdir.y) >= 0x1p-126f && fabsf(sdir.z) >= 0x1p-126f);
+    {
+        Ray r;
+        bool active = false;
+        uint32_t mine = 0, next = 0;
+        for (;;) {
+            const uint32_t idle = __ballot_sync(~0u, !active);
+            if (next < nq && (idle == ~0u || __popc(idle) >= kRefill)) {
+                if (!active) {
+                    const uint32_t k = next + __popc(idle & below);
+                    if (k < nq) {
+                        uint32_t *e = slot + k * kWaveWords;
+                        const F3 src = f3(__uint_as_float(e[0]), __uint_as_float(e[1]), __uint_as_float(e[2]));
+                        if (dir_careful || ray_needs_careful_step(src, sdir)) {
+                            e[4] &= 0x00FFFFFFu;  // alpha 0 marks the entry for the careful pass
+                        } else {
+                            ray_init(r, src, sdir);
+                            active = true;
+                            mine = k;
+                        }
+                    }
+                }
+                next += __popc(idle);
+                continue;
+            }
+            if (idle == ~0u) break;
+            if (active) {
+                const uint32_t st = ray_step<false>(J.g, r);
+                if (st != 0xFFu) {
+                    wave_shadow_done(J, slot + mine * kWaveWords, ambient, st, r.i);
+                    active = false;
+                }
+            }
+        }
+    }
+    __syncwarp();
+    for (uint32_t base = 0; base < nq; base += 32u) {
+        const uint32_t k = base + lane;
+        const bool mine = k < nq && (slot[k * kWaveWords + 4] >> 24) == 0u;
+        if (!__any_sync(~0u, mine)) continue;
+        if (mine) {
+            const uint32_t *e = slot + k * kWaveWords;
+            const March sh = hdda(J.g, f3(__uint_as_float(e[0]), __uint_as_float(e[1]), __uint_as_float(e[2])), sdir);
+            wave_shadow_done(J, e, ambient, sh.state, sh.i);
+        }
+    }
+}
+
 // First job whose tile range contains tile t (jobs sorted by tile_begin, no empty jobs).
 __device__ __forceinline__ uint32_t find_job(const Job *__restrict__ jobs, uint32_t njobs, uint32_t t,
                                              uint32_t lo) {
@@ -204,7 +416,13 @@ cudaError_t init_device_tables() {
         volatile float m = (float)d;
         h[d] = 1.0f / m;  // host IEEE division, round to nearest
     }
-    return cudaMemcpyToSymbol(wxd::g_rcp, h, sizeof h);
+    cudaError_t e = cudaMemcpyToSymbol(wxd::g_rcp, h, sizeof h);
+    // k_wave's slots: up to 8 warps x 8 tiles x 32 pixels x 5 words (40 KB).
+    const int wave_max = 8 * 8 * 32 * (int)(kWaveWords * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_wave<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, wave_max);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_wave<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, wave_max);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_wave<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, wave_max);
+    return e;
 }
 
 int max_blocks_per_sm(int kernel, bool batched, int warps_per_block) {
@@ -229,6 +447,14 @@ cudaError_t launch_pixel(const Job &job, const Tuning &t, bool disjoint, cudaStr
     cfg.numAttrs = 1;
     const uint32_t dj = disjoint ? 1u : 0u;
     if (all_modes(job.s)) return cudaLaunchKernelEx(&cfg, k_pixel<true>, job, job.tiles, dj);
+    if (t.rays > 1) {  // k_wave: t.rays tiles per warp, lanes refill
+        const uint32_t per_block = wpb * (uint32_t)t.rays;
+        cfg.gridDim = dim3((job.tiles + per_block - 1) / per_block);
+        cfg.dynamicSmemBytes = (size_t)per_block * 32u * kWaveWords * sizeof(uint32_t);
+        if (t.rays == 2) return cudaLaunchKernelEx(&cfg, k_wave<2>, job, job.tiles, dj);
+        if (t.rays == 4) return cudaLaunchKernelEx(&cfg, k_wave<4>, job, job.tiles, dj);
+        return cudaLaunchKernelEx(&cfg, k_wave<8>, job, job.tiles, dj);
+    }
     return cudaLaunchKernelEx(&cfg, k_pixel<false>, job, job.tiles, dj);
 }
 

@@ -36,7 +36,6 @@ namespace {
 constexpr uint32_t kNone = 0xFFFFFFFFu;   // no node / empty queue slot
 constexpr uint32_t kInf = 0xFFFFFFFEu;    // initial tile distance (u32::MAX - 1)
 constexpr uint32_t kChild = 0x80000000u;
-constexpr uint32_t kSpinLimit = 1u << 23;  // ~2 s of 256 ns sleeps
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
     uint32_t v;
@@ -169,7 +168,8 @@ __global__ void k_sdf_indeg(const uint32_t *__restrict__ nb, uint32_t nc, int ba
 template <int L>
 __global__ void __launch_bounds__((1 << L) * (1 << L)) k_sdf_sweep(uint32_t *d, const uint32_t *__restrict__ nb,
                                                                    uint32_t nc, int backward, uint32_t *indeg,
-                                                                   uint32_t *queue, uint32_t *ctr) {
+                                                                   uint32_t *queue, uint32_t *ctr,
+                                                                   uint32_t spin_limit) {
     constexpr int D = 1 << L, P = D + 2, N = D * D * D, T = D * D, TMAX = 7 * (D - 1);
     extern __shared__ uint32_t buf[];  // P^3
     __shared__ uint32_t s_node;
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__((1 << L) * (1 << L)) k_sdf_sweep(uint32_t *d, 
                     node = ld_acquire(&queue[ticket]);
                     if (node != kNone) break;
                     if (ld_acquire(&ctr[2]) != 0u) break;
-                    if (spin >= kSpinLimit) {
+                    if (spin >= spin_limit) {  // give up: set the error flag, every CTA then returns
                         atomicExch(&ctr[2], 1u);
                         break;
                     }
@@ -337,7 +337,7 @@ cudaError_t sdf_neighbours(int level, const int4 *org, uint32_t nc, const SdfTre
 
 template <int L>
 static cudaError_t sweep_level(uint32_t *d, const uint32_t *nb, uint32_t nc, uint32_t *indeg, uint32_t *queue,
-                               uint32_t *ctr, int num_sms, cudaStream_t st) {
+                               uint32_t *ctr, int num_sms, uint32_t spin_limit, cudaStream_t st) {
     constexpr int D = 1 << L, P = D + 2, T = D * D;
     const size_t smem = (size_t)P * P * P * 4;
     cudaError_t e = cudaFuncSetAttribute(k_sdf_sweep<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -348,18 +348,18 @@ static cudaError_t sweep_level(uint32_t *d, const uint32_t *nb, uint32_t nc, uin
         if ((e = cudaMemsetAsync(queue, 0xFF, (size_t)nc * 4, st)) != cudaSuccess) return e;
         if ((e = cudaMemsetAsync(ctr, 0, 2 * sizeof(uint32_t), st)) != cudaSuccess) return e;  // keeps ctr[2]
         k_sdf_indeg<<<grid_for(nc, 256), 256, 0, st>>>(nb, nc, pass, indeg, queue, ctr);
-        k_sdf_sweep<L><<<(unsigned)blocks, T, smem, st>>>(d, nb, nc, pass, indeg, queue, ctr);
+        k_sdf_sweep<L><<<(unsigned)blocks, T, smem, st>>>(d, nb, nc, pass, indeg, queue, ctr, spin_limit);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
 
 cudaError_t sdf_sweep(int level, uint32_t *d, const uint32_t *nb, uint32_t nc, uint32_t *indeg, uint32_t *queue,
-                      uint32_t *ctr, int num_sms, cudaStream_t st) {
+                      uint32_t *ctr, int num_sms, uint32_t spin_limit, cudaStream_t st) {
     if (!nc) return cudaSuccess;
-    if (level == 5) return sweep_level<5>(d, nb, nc, indeg, queue, ctr, num_sms, st);
-    if (level == 4) return sweep_level<4>(d, nb, nc, indeg, queue, ctr, num_sms, st);
-    return sweep_level<3>(d, nb, nc, indeg, queue, ctr, num_sms, st);
+    if (level == 5) return sweep_level<5>(d, nb, nc, indeg, queue, ctr, num_sms, spin_limit, st);
+    if (level == 4) return sweep_level<4>(d, nb, nc, indeg, queue, ctr, num_sms, spin_limit, st);
+    return sweep_level<3>(d, nb, nc, indeg, queue, ctr, num_sms, spin_limit, st);
 }
 
 cudaError_t sdf_pack_internal(const uint64_t *kid, const uint64_t *val, const uint32_t *cidx, const uint32_t *d,

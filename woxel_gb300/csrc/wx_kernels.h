@@ -43,6 +43,7 @@ struct Tuning {
     int blocks_per_sm = 0;     // 0 = as many as fit
     int tile_w = 8;            // 4, 8, 16 or 32 pixels wide (x 32/tile_w high)
     int order = 1;             // Job::order
+    int rays = 1;              // k_pixel: 1 pixel per lane; 2, 4 or 8 tiles per warp with lanes that refill (k_wave)
 };
 
 cudaError_t init_device_tables();
@@ -77,8 +78,11 @@ cudaError_t sdf_child_origins(const uint32_t *cidx, const int4 *org, uint64_t no
 cudaError_t sdf_init(const uint64_t *solid, uint64_t ncells, uint32_t *d, cudaStream_t st);
 cudaError_t sdf_neighbours(int level, const int4 *org, uint32_t nc, const SdfTree &t, uint32_t *nb, cudaStream_t st);
 // Both passes of one level; ctr[2] (not reset here) is set when a wait hit its bound.
+// spin_limit: polls (256 ns apart) a CTA makes for its container before it sets
+// the error flag ctr[2] and every CTA of the sweep returns.
+constexpr uint32_t kSdfSpinLimit = 1u << 23;  // about 2 s
 cudaError_t sdf_sweep(int level, uint32_t *d, const uint32_t *nb, uint32_t nc, uint32_t *indeg, uint32_t *queue,
-                      uint32_t *ctr, int num_sms, cudaStream_t st);
+                      uint32_t *ctr, int num_sms, uint32_t spin_limit, cudaStream_t st);
 cudaError_t sdf_pack_internal(const uint64_t *kid, const uint64_t *val, const uint32_t *cidx, const uint32_t *d,
                               uint64_t nslots, uint32_t *slot, uint32_t *err, cudaStream_t st);
 cudaError_t sdf_pack_leaves(const uint32_t *d, uint64_t ncells, uint8_t *leaf, uint2 *ovf, uint32_t cap,
