@@ -322,6 +322,26 @@ def measure_mixed(ctx, grids, dev, flush, steps, warmup):
         torch.cuda.synchronize()
         b_ms.append(e0.elapsed_time(e1))
     plan.close()
+    # Per (grid, resolution) class: plain launch time (each launch between its own events).
+    per_req = np.array(lat).reshape(len(p_ms), len(frames)).mean(axis=0)
+    classes = {}
+    for f, ms_f in zip(frames, per_req):
+        c = classes.setdefault((f.grid, f"{f.width}x{f.height}"), {"requests": 0, "rays": 0, "ms": 0.0})
+        c["requests"] += 1
+        c["rays"] += f.rays
+        c["ms"] += float(ms_f)
+    for c in classes.values():
+        c["grays_per_s"] = c["rays"] / (c["ms"] / 1e3) / 1e9
+    # Upper bound of any batching: every ray of a grid at the best rate measured on that grid
+    # (its largest frames, which fill the GPU alone).
+    best = {}
+    for (g, _), c in classes.items():
+        best[g] = max(best.get(g, 0.0), c["grays_per_s"])
+    grid_rays = {}
+    for f in frames:
+        grid_rays[f.grid] = grid_rays.get(f.grid, 0) + f.rays
+    bound_s = sum(r / (best[g] * 1e9) for g, r in grid_rays.items())
+    bound = rays / bound_s / 1e9
     lat.sort()
     pm, bm = statistics.mean(p_ms), statistics.mean(b_ms)
     return {
@@ -335,6 +355,12 @@ def measure_mixed(ctx, grids, dev, flush, steps, warmup):
                     "request_latency_ms": {"p50": bm, "p99": bm, "note": "every request completes with the batch"},
                     "launches_per_step": 1, "cuda_graph": True},
         "speedup": pm / bm,
+        "classes": {f"{g} {res}": c for (g, res), c in sorted(classes.items())},
+        "bound": {"value": bound, "unit": "Grays/s", "speedup_over_plain": bound / (rays / (pm / 1e3) / 1e9),
+                  "best_grays_per_s": best,
+                  "note": "every request's rays at the best per-grid rate of the plain launches (largest frames); "
+                          "no batching can beat it, so the attainable speed-up over plain is bounded by it"},
+        "batched_of_bound": (rays / (bm / 1e3) / 1e9) / bound,
     }
 
 

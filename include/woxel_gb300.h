@@ -173,6 +173,12 @@ int wx_grid_build_gpu(wx_ctx *ctx, const wx_topology *topo, wx_grid **out);
  * default, 2^23, about 2 s). No counterpart in the reference, whose failures
  * panic (wgpu_context.rs:44-101). */
 int wx_ctx_set_sdf_wait_limit(wx_ctx *ctx, uint32_t polls);
+/* Fault injection for tests of callers' error paths: the library's next
+ * `count` device or page-locked host allocations (grid pools, staging, job
+ * tables, server arena and slots, GPU SDF temporaries) fail as an exhausted
+ * device would, without calling CUDA: the call reports WX_ERR_OOM, frees what
+ * it had allocated and leaves the context usable. 0 stops injecting. */
+int wx_inject_alloc_failures(uint32_t count);
 int wx_grid_release(wx_ctx *ctx, wx_grid *grid);
 /* Attaches level-set values for WX_MODE_SURFACE: one float per leaf voxel
  * (n3 * 512, DFS leaf order, voxel order x<<6 | y<<3 | z), the signed distance
@@ -267,7 +273,7 @@ int wx_batch_destroy(wx_batch *batch);
  * different streams, or from other host threads before earlier work finished)
  * race; the caller must serialise them (calls on one stream are ordered). */
 #define WX_NOALLOC_MAX_FRAMES 256
-#define WX_NOALLOC_SCRATCH_BYTES 96512 /* 256 + 256 frames x 376-byte table entries */
+#define WX_NOALLOC_SCRATCH_BYTES 98560 /* 256 + 256 frames x 384-byte table entries */
 int wx_render_batch_noalloc(const wx_frame *frames, uint32_t n, void *stream);
 
 /* ---- serving: continuous batching of render requests (no counterpart in the
@@ -311,6 +317,8 @@ typedef struct wx_server_stats {
     uint64_t rays_done;        /* dispatched pixels of completed requests */
     uint64_t arena_bytes, arena_in_use, arena_peak;
     uint64_t pending, active;
+    uint64_t tiles_cancelled_queued;   /* tiles of cancelled requests never launched */
+    uint64_t tiles_cancelled_launched; /* tiles skipped by launches already on the GPU */
 } wx_server_stats;
 
 /* Creates the scheduler and allocates the output arena (budget minus the
@@ -321,7 +329,14 @@ int wx_server_create(wx_ctx *ctx, const wx_server_config *cfg, wx_server **out);
 int wx_server_add_grid(wx_server *srv, const wx_grid *grid, uint32_t *grid_id);
 /* Queues a request (never blocks on the GPU). WX_ERR_BUDGET if it could never fit. */
 int wx_server_submit(wx_server *srv, const wx_request *req, uint64_t *ticket);
-/* Cancels a request that has not been admitted yet (its result reports WX_ERR_CANCELLED). */
+/* Cancels a request (its result reports WX_ERR_CANCELLED and has no buffers).
+ * Pending: it is never admitted. Admitted: its tiles not yet launched are
+ * dropped, and launches already on the GPU skip its remaining tiles as soon as
+ * the cancellation reaches the device (a cancel table the batched kernel reads
+ * before each tile, written concurrently with the launches); the result arrives
+ * once no launch refers to the request. The other requests are not affected.
+ * WX_ERR_INVALID for an unknown or already finished request. The reference has
+ * no counterpart (its render loop cannot stop a dispatch). */
 int wx_server_cancel(wx_server *srv, uint64_t ticket);
 /* Moves up to max finished results into out; waits up to wait_ms for the first. */
 int wx_server_poll(wx_server *srv, wx_result *out, uint32_t max, uint32_t *n, int wait_ms);

@@ -398,11 +398,17 @@ def render_batch_noalloc(frames: Sequence, stream=None) -> None:
     """wx_render_batch_noalloc: a batch rendered without any allocation or context.
 
     For callers that cannot allocate device memory while rendering; scratch is a
-    fixed 96,512-byte device array inside the library (at most 256 frames a call).
+    fixed 98,560-byte device array inside the library (at most 256 frames a call).
     The first call on a device sets that device up; overlapping calls race.
     """
     arr = Context._frames(frames)
     check(lib().wx_render_batch_noalloc(arr, len(frames), None if stream is None else int(stream)))
+
+
+def inject_alloc_failures(count: int) -> None:
+    """wx_inject_alloc_failures: the library's next `count` device or page-locked allocations fail
+    as out of memory (testing error paths); 0 stops injecting."""
+    check(lib().wx_inject_alloc_failures(count))
 
 
 class Batch:

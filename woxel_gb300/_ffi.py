@@ -68,7 +68,8 @@ class wx_server_stats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("cancelled", C.c_uint64),
                 ("launches", C.c_uint64), ("rays_done", C.c_uint64), ("arena_bytes", C.c_uint64),
                 ("arena_in_use", C.c_uint64), ("arena_peak", C.c_uint64), ("pending", C.c_uint64),
-                ("active", C.c_uint64)]
+                ("active", C.c_uint64), ("tiles_cancelled_queued", C.c_uint64),
+                ("tiles_cancelled_launched", C.c_uint64)]
 
 
 class wx_vdb_info(C.Structure):
@@ -101,6 +102,7 @@ SIGNATURES = {
     "wx_ctx_set_tuning": (INT, [P, C.POINTER(wx_tuning)]),
     "wx_ctx_get_tuning": (INT, [P, C.POINTER(wx_tuning)]),
     "wx_ctx_set_sdf_wait_limit": (INT, [P, C.c_uint32]),
+    "wx_inject_alloc_failures": (INT, [C.c_uint32]),
     "wx_render_batch": (INT, [P, C.POINTER(wx_frame), U32, P]),
     "wx_batch_create": (INT, [P, C.POINTER(wx_frame), U32, C.POINTER(P)]),
     "wx_batch_launch": (INT, [P, P]),

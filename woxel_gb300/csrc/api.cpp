@@ -30,6 +30,7 @@
 #include <thread>
 #include <vector>
 
+#include "wx_alloc.h"
 #include "wx_common.h"
 #include "wx_kernels.h"
 
@@ -77,6 +78,17 @@ struct wx_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
+
+namespace wx {
+// Injected allocation failures (wx_inject_alloc_failures), taken one per allocation.
+static std::atomic<uint32_t> g_alloc_failures{0};
+bool take_injected_alloc_failure() {
+    uint32_t n = g_alloc_failures.load(std::memory_order_relaxed);
+    while (n != 0 && !g_alloc_failures.compare_exchange_weak(n, n - 1, std::memory_order_relaxed)) {
+    }
+    return n != 0;
+}
+}  // namespace wx
 
 namespace {
 
@@ -263,7 +275,7 @@ int alloc_grid(wx_ctx *ctx, const std::vector<int4> &o5, uint64_t n5, uint64_t n
                  b4 = align(n4 * 4096ull * 4), b3 = align(n3 * 512ull), bo = align(n_ovf * 8);
     gr->bytes = b_o5 + b5 + b4 + b3 + bo;
     gr->device = ctx->device;
-    cudaError_t e = cudaMalloc(&gr->dev, gr->bytes);
+    cudaError_t e = wx::dev_alloc(&gr->dev, gr->bytes);
     if (e != cudaSuccess) {
         delete gr;
         return cuda_fail(ctx, e, "cudaMalloc(node pools)");
@@ -417,11 +429,11 @@ int wx_ctx_create(int device, wx_ctx **out) {
     if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
         return cleanup(e, "cudaDeviceGetAttribute");
     if ((e = wxk::init_device_tables()) != cudaSuccess) return cleanup(e, "init_device_tables");
-    if ((e = cudaMalloc(&c->counters, kCounterSlots * sizeof(uint32_t))) != cudaSuccess)
+    if ((e = wx::dev_alloc(&c->counters, kCounterSlots * sizeof(uint32_t))) != cudaSuccess)
         return cleanup(e, "cudaMalloc(counters)");
     if ((e = cudaMemset(c->counters, 0, kCounterSlots * sizeof(uint32_t))) != cudaSuccess)
         return cleanup(e, "cudaMemset(counters)");
-    if ((e = cudaMalloc(&c->check, 4 * sizeof(unsigned long long))) != cudaSuccess)
+    if ((e = wx::dev_alloc(&c->check, 4 * sizeof(unsigned long long))) != cudaSuccess)
         return cleanup(e, "cudaMalloc(check)");
     if ((e = cudaEventCreateWithFlags(&c->jobs_done, cudaEventDisableTiming)) != cudaSuccess)
         return cleanup(e, "cudaEventCreate");
@@ -460,6 +472,11 @@ int wx_ctx_set_tuning(wx_ctx *ctx, const wx_tuning *t) {
     ctx->tuning.tile_w = t->tile_width;
     ctx->tuning.order = t->tile_order;
     ctx->tuning.rays = t->rays_per_lane;
+    return WX_OK;
+}
+
+int wx_inject_alloc_failures(uint32_t count) {
+    wx::g_alloc_failures.store(count, std::memory_order_relaxed);
     return WX_OK;
 }
 
@@ -690,7 +707,7 @@ int wx_grid_build_gpu(wx_ctx *ctx, const wx_topology *t, wx_grid **out) {
                   {&nb, nmax * 27 * 4},        {&indeg, nmax * 4},         {&queue, nmax * 4},
                   {&ctr, 8 * 4}};
     for (auto &a : allocs)
-        if (a.bytes) WX_CUDA(ctx, cudaMalloc(&a.b->p, a.bytes));
+        if (a.bytes) WX_CUDA(ctx, wx::dev_alloc(&a.b->p, a.bytes));
     struct Up {
         DevBuf *b;
         const void *src;
@@ -894,7 +911,7 @@ int wx_grid_set_values(wx_ctx *ctx, wx_grid *grid, const float *values, float ba
         return fail(ctx, WX_ERR_INVALID, "wx_grid_set_values: band must be positive and finite");
     WX_CUDA(ctx, cudaSetDevice(grid->device));
     const size_t bytes = (size_t)grid->info.n3 * wx::kN3Slots * sizeof(float);
-    if (!grid->values && bytes) WX_CUDA(ctx, cudaMalloc(&grid->values, bytes));
+    if (!grid->values && bytes) WX_CUDA(ctx, wx::dev_alloc(&grid->values, bytes));
     if (bytes) WX_CUDA(ctx, cudaMemcpy(grid->values, values, bytes, cudaMemcpyHostToDevice));
     grid->g.values = grid->values;
     grid->g.band = band;
@@ -948,7 +965,7 @@ int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, u
             }
             ctx->stage = nullptr;
             ctx->stage_bytes = 0;
-            WX_CUDA(ctx, cudaMalloc(&ctx->stage, need));
+            WX_CUDA(ctx, wx::dev_alloc(&ctx->stage, need));
             ctx->stage_bytes = need;
         }
         char *b = static_cast<char *>(ctx->stage);
@@ -1029,8 +1046,8 @@ int wx_render_batch(wx_ctx *ctx, const wx_frame *frames, uint32_t n, void *strea
         ctx->jobs_host = nullptr;
         ctx->jobs_cap = 0;
         const size_t cap = std::max<size_t>(jobs.size(), 256);
-        WX_CUDA(ctx, cudaMalloc(&ctx->jobs_dev, cap * sizeof(wxk::Job)));
-        WX_CUDA(ctx, cudaMallocHost(&ctx->jobs_host, cap * sizeof(wxk::Job)));
+        WX_CUDA(ctx, wx::dev_alloc(&ctx->jobs_dev, cap * sizeof(wxk::Job)));
+        WX_CUDA(ctx, wx::pinned_alloc(&ctx->jobs_host, cap * sizeof(wxk::Job)));
         ctx->jobs_cap = cap;
     }
     memcpy(ctx->jobs_host, jobs.data(), jobs.size() * sizeof(wxk::Job));
@@ -1061,12 +1078,12 @@ int wx_batch_create(wx_ctx *ctx, const wx_frame *frames, uint32_t n, wx_batch **
         return cuda_fail(ctx, e, what);
     };
     cudaError_t e;
-    if ((e = cudaMalloc(&b->jobs_dev, std::max<size_t>(jobs.size(), 1) * sizeof(wxk::Job))) != cudaSuccess)
+    if ((e = wx::dev_alloc(&b->jobs_dev, std::max<size_t>(jobs.size(), 1) * sizeof(wxk::Job))) != cudaSuccess)
         return bail(e, "cudaMalloc(job table)");
     if (!jobs.empty() &&
         (e = cudaMemcpy(b->jobs_dev, jobs.data(), jobs.size() * sizeof(wxk::Job), cudaMemcpyHostToDevice)) != cudaSuccess)
         return bail(e, "cudaMemcpy(job table)");
-    if ((e = cudaMalloc(&b->counter, sizeof(uint32_t))) != cudaSuccess) return bail(e, "cudaMalloc(counter)");
+    if ((e = wx::dev_alloc(&b->counter, sizeof(uint32_t))) != cudaSuccess) return bail(e, "cudaMalloc(counter)");
     // Capture counter reset + persistent launch into a graph, replayed by wx_batch_launch.
     cudaStream_t cs;
     if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");

@@ -356,9 +356,13 @@ __device__ __forceinline__ uint32_t find_job(const Job *__restrict__ jobs, uint3
 // Persistent warps drawing whole tiles from a global queue (one atomic per
 // 32 rays). Tiles are numbered job by job; a warp's successive tiles increase,
 // so its job search starts at the previous job.
+// Batched launches may carry a cancel table (the server's): a job whose
+// cancel_id has been written to cancel[cancel_slot] (by the host, while the
+// launch runs) has its remaining tiles skipped, which `skipped` counts.
 template <bool kBatched, bool kAll>
 __global__ void WX_RAY_BOUNDS k_persistent(const Job *__restrict__ jobs, uint32_t njobs, const __grid_constant__ Job job0,
-                             uint32_t total_tiles, uint32_t *__restrict__ ctr) {
+                             uint32_t total_tiles, uint32_t *__restrict__ ctr, const uint32_t *cancel,
+                             uint32_t *skipped) {
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t cur_job = 0;
     for (;;) {
@@ -369,6 +373,17 @@ __global__ void WX_RAY_BOUNDS k_persistent(const Job *__restrict__ jobs, uint32_
         if (kBatched) {
             cur_job = find_job(jobs, njobs, t, cur_job);
             const Job &J = jobs[cur_job];
+            if (cancel) {
+                uint32_t id = 0, c = 0;
+                if (lane == 0) {
+                    id = __ldg(&J.cancel_id);
+                    if (id) asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(cancel + __ldg(&J.cancel_slot)));
+                }
+                if (__shfl_sync(~0u, id != 0u && c == id, 0)) {
+                    if (lane == 0 && skipped) atomicAdd(skipped, 1u);
+                    continue;
+                }
+            }
             render_pixel<kAll>(J, t - J.tile_begin + J.tile_off, lane, true);
         } else {
             render_pixel<kAll>(job0, t, lane, true);
@@ -471,22 +486,27 @@ cudaError_t launch_persistent(const Job &job, uint32_t *ctr, const Tuning &t, in
     if (e != cudaSuccess) return e;
     const int blocks = grid_blocks(t, false, num_sms, job.tiles);
     if (all_modes(job.s))
-        k_persistent<false, true><<<blocks, 32 * t.warps_per_block, 0, st>>>(nullptr, 1, job, job.tiles, ctr);
+        k_persistent<false, true><<<blocks, 32 * t.warps_per_block, 0, st>>>(nullptr, 1, job, job.tiles, ctr, nullptr,
+                                                                            nullptr);
     else
-        k_persistent<false, false><<<blocks, 32 * t.warps_per_block, 0, st>>>(nullptr, 1, job, job.tiles, ctr);
+        k_persistent<false, false><<<blocks, 32 * t.warps_per_block, 0, st>>>(nullptr, 1, job, job.tiles, ctr, nullptr,
+                                                                             nullptr);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batched(const Job *jobs_dev, uint32_t njobs, uint32_t total_tiles, uint32_t *ctr,
-                           const Tuning &t, int num_sms, bool all, cudaStream_t st) {
+                           const Tuning &t, int num_sms, bool all, cudaStream_t st, const uint32_t *cancel,
+                           uint32_t *skipped) {
     cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     Job dummy{};
     const int blocks = grid_blocks(t, true, num_sms, total_tiles);
     if (all)
-        k_persistent<true, true><<<blocks, 32 * t.warps_per_block, 0, st>>>(jobs_dev, njobs, dummy, total_tiles, ctr);
+        k_persistent<true, true><<<blocks, 32 * t.warps_per_block, 0, st>>>(jobs_dev, njobs, dummy, total_tiles, ctr,
+                                                                           cancel, skipped);
     else
-        k_persistent<true, false><<<blocks, 32 * t.warps_per_block, 0, st>>>(jobs_dev, njobs, dummy, total_tiles, ctr);
+        k_persistent<true, false><<<blocks, 32 * t.warps_per_block, 0, st>>>(jobs_dev, njobs, dummy, total_tiles, ctr,
+                                                                            cancel, skipped);
     return cudaGetLastError();
 }
 
@@ -529,7 +549,7 @@ cudaError_t check_division(uint32_t max_m, unsigned long long *out_dev, cudaStre
 // deadline). wx_render_batch needs a context whose scratch (queue counters,
 // frame table) comes from cudaMalloc. This entry point instead keeps its
 // scratch in the fixed device array below, which the library declares
-// statically: every GPU that loads the library holds these 96,512 bytes until
+// statically: every GPU that loads the library holds these 98,560 bytes until
 // the process exits. Layout: the tile-queue counter at byte 0, the frame
 // (job) table from byte 256, room for WX_NOALLOC_MAX_FRAMES frames.
 // ---------------------------------------------------------------------------

@@ -26,6 +26,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "wx_alloc.h"
 #include "wx_common.h"
 #include "wx_kernels.h"
 
@@ -42,7 +43,7 @@ class Arena {
     cudaError_t init(size_t bytes) {
         size_ = bytes & ~(size_t)255;
         if (size_ == 0) return cudaSuccess;
-        cudaError_t e = cudaMalloc(&base_, size_);
+        cudaError_t e = wx::dev_alloc(&base_, size_);
         if (e == cudaSuccess) free_[0] = size_;
         return e;
     }
@@ -113,12 +114,16 @@ struct Slot {
     cudaEvent_t ev = nullptr;
     wxk::Job *jobs_host = nullptr;
     wxk::Job *jobs_dev = nullptr;
-    uint32_t *counter = nullptr;
+    uint32_t *counter = nullptr;   // [0] tile queue, [1] tiles skipped for cancelled requests
+    uint32_t *skipped_host = nullptr;  // page-locked copy of counter[1] after the launch
     bool busy = false;
     std::vector<std::pair<Req *, uint32_t>> parts;
 };
 
 constexpr uint32_t kTileW = 8, kTileH = 4;
+// Cancel table: a request's tiles in launches already on the GPU are skipped
+// once its ticket (low 32 bits) is written at ticket % kCancelSlots.
+constexpr uint32_t kCancelSlots = 65536;
 
 }  // namespace
 
@@ -134,6 +139,8 @@ struct wx_server {
     std::deque<Req *> pending, active, done_q;
     std::unordered_map<uint64_t, Req *> reqs;
     std::vector<Slot> slots;
+    uint32_t *cancel_dev = nullptr, *cancel_host = nullptr;  // the cancel table and its page-locked source
+    cudaStream_t ctl = nullptr;                             // carries cancel writes while launches run
     std::thread th;
     bool stop = false, arena_ready = false;
     uint64_t next_ticket = 1;
@@ -155,7 +162,7 @@ struct wx_server {
     // Tiles of q are retired (rendered, or given up after an error); the
     // request finishes once every tile is, so no launch still refers to it.
     void retire_tiles(Req *q, uint32_t n, bool ok) {
-        if (!ok) q->status = WX_ERR_CUDA;
+        if (!ok && q->status == WX_OK) q->status = WX_ERR_CUDA;
         q->done_tiles += n;
         if (q->done_tiles == q->tiles && q->state == RState::Active) finish(q, q->status);
     }
@@ -168,6 +175,7 @@ struct wx_server {
             const cudaError_t e = cudaEventQuery(s.ev);
             if (e == cudaErrorNotReady) continue;
             if (e != cudaSuccess) cudaGetLastError();
+            else st.tiles_cancelled_launched += *s.skipped_host;
             for (auto &p : s.parts) retire_tiles(p.first, p.second, e == cudaSuccess);
             s.parts.clear();
             s.busy = false;
@@ -200,9 +208,10 @@ struct wx_server {
         const bool fifo = cfg.flags & WX_SERVE_FIFO;
         uint32_t budget = fifo ? UINT32_MAX : cfg.slice_tiles, tiles = 0, n = 0;
         for (Req *q : active) {
-            if (q->next < q->tiles && q->status != WX_OK) {  // failed earlier: give up its remaining tiles
+            if (q->next < q->tiles && q->status != WX_OK) {  // failed or cancelled: give up its remaining tiles
                 const uint32_t rest = q->tiles - q->next;
                 q->next = q->tiles;
+                if (q->status == WX_ERR_CANCELLED) st.tiles_cancelled_queued += rest;
                 retire_tiles(q, rest, false);
             }
             if (q->next >= q->tiles) continue;
@@ -223,6 +232,8 @@ struct wx_server {
             j.rgba = reinterpret_cast<uint32_t *>(q->rgba);
             j.hits = q->hits;
             j.s = q->r.state;
+            j.cancel_slot = (uint32_t)(q->ticket % kCancelSlots);
+            j.cancel_id = (uint32_t)q->ticket;
             s.parts.emplace_back(q, take);
             q->next += take;
             tiles += take;
@@ -233,9 +244,12 @@ struct wx_server {
         if (n == 0) return false;
         wxk::Tuning t;
         cudaError_t e = cudaMemcpyAsync(s.jobs_dev, s.jobs_host, n * sizeof(wxk::Job), cudaMemcpyHostToDevice, s.stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s.counter, 0, 2 * sizeof(uint32_t), s.stream);
         if (e == cudaSuccess)
             e = wxk::launch_batched(s.jobs_dev, n, tiles, s.counter, t, num_sms, wxk::all_modes(s.jobs_host, n),
-                                    s.stream);
+                                    s.stream, cancel_dev, s.counter + 1);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s.skipped_host, s.counter + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s.stream);
         if (e == cudaSuccess) e = cudaEventRecord(s.ev, s.stream);
         if (e != cudaSuccess) {
             cudaGetLastError();
@@ -313,10 +327,17 @@ int wx_server_create(wx_ctx *ctx, const wx_server_config *cfg, wx_server **out) 
     for (Slot &sl : s->slots) {
         if ((e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
         if ((e = cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "event");
-        if ((e = cudaMallocHost(&sl.jobs_host, c.max_frames * sizeof(wxk::Job))) != cudaSuccess) return bail(e, "jobs");
-        if ((e = cudaMalloc(&sl.jobs_dev, c.max_frames * sizeof(wxk::Job))) != cudaSuccess) return bail(e, "jobs");
-        if ((e = cudaMalloc(&sl.counter, 256)) != cudaSuccess) return bail(e, "counter");
+        if ((e = wx::pinned_alloc(&sl.jobs_host, c.max_frames * sizeof(wxk::Job))) != cudaSuccess) return bail(e, "jobs");
+        if ((e = wx::dev_alloc(&sl.jobs_dev, c.max_frames * sizeof(wxk::Job))) != cudaSuccess) return bail(e, "jobs");
+        if ((e = wx::dev_alloc(&sl.counter, 256)) != cudaSuccess) return bail(e, "counter");
+        if ((e = wx::pinned_alloc(&sl.skipped_host, sizeof(uint32_t))) != cudaSuccess) return bail(e, "counter");
+        *sl.skipped_host = 0;
     }
+    if ((e = wx::dev_alloc(&s->cancel_dev, kCancelSlots * sizeof(uint32_t))) != cudaSuccess) return bail(e, "cancel");
+    if ((e = wx::pinned_alloc(&s->cancel_host, kCancelSlots * sizeof(uint32_t))) != cudaSuccess)
+        return bail(e, "cancel");
+    if ((e = cudaMemset(s->cancel_dev, 0, kCancelSlots * sizeof(uint32_t))) != cudaSuccess) return bail(e, "cancel");
+    if ((e = cudaStreamCreateWithFlags(&s->ctl, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
     s->th = std::thread([s] { s->loop(); });
     *out = s;
     return WX_OK;
@@ -393,9 +414,29 @@ int wx_server_cancel(wx_server *s, uint64_t ticket) {
     auto it = s->reqs.find(ticket);
     if (it == s->reqs.end()) return sfail(WX_ERR_INVALID, "wx_server_cancel: unknown ticket");
     Req *q = it->second;
-    if (q->state != RState::Pending) return sfail(WX_ERR_INVALID, "wx_server_cancel: request already admitted");
-    s->pending.erase(std::find(s->pending.begin(), s->pending.end(), q));
-    s->finish(q, WX_ERR_CANCELLED);
+    if (q->state == RState::Pending) {
+        s->pending.erase(std::find(s->pending.begin(), s->pending.end(), q));
+        s->finish(q, WX_ERR_CANCELLED);
+        return WX_OK;
+    }
+    if (q->state != RState::Active) return sfail(WX_ERR_INVALID, "wx_server_cancel: request already finished");
+    if (q->status == WX_OK) {
+        // Tiles not yet launched are dropped by the scheduler; launches on the GPU
+        // skip the rest once the ticket lands in the cancel table (copied on the
+        // control stream, concurrently with them). The request finishes with
+        // WX_ERR_CANCELLED when no launch refers to it any more.
+        q->status = WX_ERR_CANCELLED;
+        const uint32_t slot = (uint32_t)(q->ticket % kCancelSlots);
+        s->cancel_host[slot] = (uint32_t)q->ticket;
+        int prev = -1;
+        cudaGetDevice(&prev);
+        if (prev != s->device) cudaSetDevice(s->device);
+        const cudaError_t e = cudaMemcpyAsync(s->cancel_dev + slot, s->cancel_host + slot, sizeof(uint32_t),
+                                              cudaMemcpyHostToDevice, s->ctl);
+        if (prev != s->device && prev >= 0) cudaSetDevice(prev);
+        if (e != cudaSuccess) cudaGetLastError();  // the launched tiles then just render
+    }
+    s->cv_work.notify_one();
     return WX_OK;
 }
 
@@ -530,7 +571,14 @@ int wx_server_destroy(wx_server *s) {
         if (sl.jobs_host) cudaFreeHost(sl.jobs_host);
         if (sl.jobs_dev) cudaFree(sl.jobs_dev);
         if (sl.counter) cudaFree(sl.counter);
+        if (sl.skipped_host) cudaFreeHost(sl.skipped_host);
     }
+    if (s->ctl) {
+        cudaStreamSynchronize(s->ctl);
+        cudaStreamDestroy(s->ctl);
+    }
+    if (s->cancel_dev) cudaFree(s->cancel_dev);
+    if (s->cancel_host) cudaFreeHost(s->cancel_host);
     s->arena.destroy();
     for (auto &kv : s->reqs) delete kv.second;
     delete s;

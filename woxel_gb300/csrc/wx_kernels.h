@@ -35,6 +35,9 @@ struct Job {
     uint32_t *rgba;
     wx_hit *hits;
     wx_state_uniform s;
+    // Cancellation (batched launches given a cancel table): the job's tiles are
+    // skipped once cancel[cancel_slot] == cancel_id (nonzero). 0 = never.
+    uint32_t cancel_slot, cancel_id;
 };
 
 struct Tuning {
@@ -53,8 +56,11 @@ int max_blocks_per_sm(int kernel, bool batched, int warps_per_block);
 cudaError_t launch_pixel(const Job &job, const Tuning &t, bool disjoint, cudaStream_t st);
 cudaError_t launch_persistent(const Job &job, uint32_t *ctr, const Tuning &t, int num_sms, cudaStream_t st);
 // all: some job renders mode 4 or 5 (the kernels compiled for every mode).
+// cancel (may be NULL): the table the jobs' cancel_slot index; skipped (may be
+// NULL) counts the tiles skipped for a cancelled job (the caller clears it).
 cudaError_t launch_batched(const Job *jobs_dev, uint32_t njobs, uint32_t total_tiles, uint32_t *ctr,
-                           const Tuning &t, int num_sms, bool all, cudaStream_t st);
+                           const Tuning &t, int num_sms, bool all, cudaStream_t st,
+                           const uint32_t *cancel = nullptr, uint32_t *skipped = nullptr);
 // Modes 4 (glossy) and 5 (zero crossing) need the kernels compiled for every mode.
 bool all_modes(const wx_state_uniform &s);
 bool all_modes(const Job *jobs, size_t n);
