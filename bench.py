@@ -364,36 +364,31 @@ def measure_mixed(ctx, grids, dev, flush, steps, warmup):
     }
 
 
-def run_serve(args):
-    """Serving: open-loop Poisson arrivals over 8 resident grids (4 sphere-generator
-    grids with distinct seeds, 4 2000-sphere grids with seeds 2..5), the resolution mix of the
-    mixed requests,
-    HBM budget 150 GB. Each rate is replayed on the continuous-batching server and on the FIFO
-    single-request server; reports p50/p99 request latency and served Grays/s."""
-    import torch
-
+def serve_sweep(ctx, rates, duration, slice_tiles=65536, timeout=300.0):
+    """Serving: open-loop Poisson arrivals over 8 resident grids (4 sphere-generator grids with
+    distinct seeds, 4 2000-sphere grids with seeds 2..5, built on the GPU), the resolution mix
+    of the mixed requests, HBM budget 150 GB. Each rate is replayed on the continuous-batching
+    server and on the FIFO single-request server; reports p50/p99 request latency and served
+    Grays/s."""
     import woxel_gb300 as wx
     from woxel_gb300 import workloads as W
 
-    torch.cuda.set_device(0)
-    ctx = wx.Context(0)
     t0 = time.perf_counter()
     grids, kinds = [], []
     for s in range(4):
-        grids.append(ctx.build_grid(W.sphere_topology(s)))
+        grids.append(ctx.build_grid(W.sphere_topology(s), gpu=True))
         kinds.append("sphere")
     for s in range(2, 6):
-        grids.append(ctx.build_grid(W.spheres_topology(s)))
+        grids.append(ctx.build_grid(W.spheres_topology(s), gpu=True))
         kinds.append("spheres")
     grid_bytes = sum(g.info["device_bytes"] for g in grids)
     log(f"[serve] 8 grids, {grid_bytes / 1e9:.2f} GB of node pools, built in {time.perf_counter() - t0:.1f}s")
-    rates = [float(r) for r in args.serve_rates.split(",")]
     budget = 150 * 10**9
 
     def trace(rate, seed):
         rng = np.random.default_rng(seed)
-        n = max(1, int(rng.poisson(rate * args.serve_duration)))
-        arr = np.sort(rng.uniform(0, args.serve_duration, size=n))
+        n = max(1, int(rng.poisson(rate * duration)))
+        arr = np.sort(rng.uniform(0, duration, size=n))
         reqs, rays = [], 0
         for i in range(n):
             gid = int(rng.integers(0, len(grids)))
@@ -408,38 +403,132 @@ def run_serve(args):
 
     out = []
     for mode in ("batched", "fifo"):
-        srv = wx.Server(ctx, budget_bytes=budget, max_inflight=2, slice_tiles=args.serve_slice, fifo=(mode == "fifo"))
+        srv = wx.Server(ctx, budget_bytes=budget, max_inflight=2, slice_tiles=slice_tiles, fifo=(mode == "fifo"))
         for g in grids:
             srv.add_grid(g)
-        # warm-up: a few requests
-        wreqs, warr, _ = trace(50.0, 1)
+        wreqs, _, _ = trace(50.0, 1)  # warm-up: a few requests
         srv.replay(wreqs[:8], [0.0] * min(8, len(wreqs)), release=True)
         for k, rate in enumerate(rates):
             reqs, arr, rays = trace(rate, 1000 + k)
             t1 = time.perf_counter()
-            res = srv.replay(reqs, arr, release=True, timeout_s=args.serve_timeout)
+            res = srv.replay(reqs, arr, release=True, timeout_s=timeout)
             wall = time.perf_counter() - t1
             lat = np.array([r.t_done - r.t_submit for r in res]) * 1e3
             first = min(r.t_submit for r in res)
             last = max(r.t_done for r in res)
-            out.append({"mode": mode, "rate_req_s": rate, "requests": len(reqs), "offered_grays_per_s": rays / args.serve_duration / 1e9,
-                        "served_grays_per_s": rays / (last - first) / 1e9, "latency_ms_p50": float(np.percentile(lat, 50)),
+            out.append({"mode": mode, "rate_req_s": rate, "requests": len(reqs),
+                        "offered_grays_per_s": rays / duration / 1e9,
+                        "served_grays_per_s": rays / (last - first) / 1e9,
+                        "latency_ms_p50": float(np.percentile(lat, 50)),
                         "latency_ms_p99": float(np.percentile(lat, 99)), "wall_s": wall})
             log(f"[serve] {mode} {rate:.0f} req/s: {out[-1]}")
-        stats = srv.stats
-        out[-1]["launches_total"] = stats["launches"]
+        out[-1]["launches_total"] = srv.stats["launches"]
         srv.close()
+    for g in grids:
+        g.release()
     best = max((o for o in out if o["mode"] == "batched"), key=lambda o: o["served_grays_per_s"])
     fifo_best = max((o for o in out if o["mode"] == "fifo"), key=lambda o: o["served_grays_per_s"])
-    print(json.dumps({
-        "metric": "served_primary_ray_grays_per_s", "value": best["served_grays_per_s"], "unit": "Grays/s",
-        "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "serving: Poisson arrivals over 8 resident grids (4 sphere, 4 2000-sphere), "
-                               "resolutions 256x256..3840x2160, mode 3", "budget_bytes": budget,
-                   "grid_bytes": grid_bytes, "duration_s_per_rate": args.serve_duration,
-                   "slice_tiles": args.serve_slice, "max_inflight": 2},
-        "fifo_value": fifo_best["served_grays_per_s"], "sweep": out,
-    }), flush=True)
+    return {"workload": "serving: Poisson arrivals over 8 resident grids (4 sphere, 4 2000-sphere), "
+                        "resolutions 256x256..3840x2160, mode 3",
+            "value": best["served_grays_per_s"], "fifo_value": fifo_best["served_grays_per_s"], "unit": "Grays/s",
+            "speedup_over_fifo": best["served_grays_per_s"] / fifo_best["served_grays_per_s"],
+            "budget_bytes": budget, "grid_bytes": grid_bytes, "duration_s_per_rate": duration,
+            "slice_tiles": slice_tiles, "max_inflight": 2, "sweep": out}
+
+
+def run_serve(args):
+    """--serve: the serving sweep alone, as its own JSON line."""
+    import torch
+
+    import woxel_gb300 as wx
+
+    torch.cuda.set_device(0)
+    ctx = wx.Context(0)
+    r = serve_sweep(ctx, [float(x) for x in args.serve_rates.split(",")], args.serve_duration, args.serve_slice,
+                    args.serve_timeout)
+    print(json.dumps({"metric": "served_primary_ray_grays_per_s", "value": r.pop("value"), "unit": "Grays/s",
+                      "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+                      "config": {"workload": r.pop("workload")}, **r}), flush=True)
+
+
+def extra_workload(ctx, name, dev, flush, steps, warmup):
+    """A benchmark workload besides the main one (the r=64 sphere at 640x480, the 4096^3 noise
+    grid at 3840x2160), measured like the main one: grid built on the GPU, autotuned on its
+    frames, plain per-frame launches, L2 flushed between steps; the roofline from the oracle's
+    node-visit bytes on a tile sample."""
+    import torch
+
+    from woxel_gb300 import workloads as W
+
+    wl = W.workload(name)
+    topo = wl.grids[wl.frames[0].grid]()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    grid = ctx.build_grid(topo, gpu=True)
+    torch.cuda.synchronize(dev)
+    t_build = time.perf_counter() - t0
+    frames = wl.frames
+    states = [f.state() for f in frames]
+    outs = [torch.empty(f.width * f.height * 4, dtype=torch.uint8, device=dev) for f in frames]
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    saved = ctx.tuning
+    tuned = ctx.autotune([(grid, st, f.width, f.height, o, None) for f, st, o in list(zip(frames, states, outs))[:4]],
+                         reps=2)
+
+    def step():
+        for f, st, o in zip(frames, states, outs):
+            ctx.render(grid, st, f.width, f.height, o, None, stream=sh)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    ms = []
+    with ClockSampler(dev.index or 0) as clk:
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms.append(e0.elapsed_time(e1))
+    m = statistics.mean(ms)
+    rays = wl.rays
+    value = rays / (m / 1e3) / 1e9
+    tn = ctx.tuning
+    kernel = "k_persistent" if tn["kernel"] == 0 else ("k_wave" if tn["rays_per_lane"] > 1 else "k_pixel")
+    ctx.set_tuning(**saved)
+    info = grid.info
+    grid.release()
+    # Algorithmic bytes: the oracle's node-visit counts on a tile sample of the same frames.
+    view, view_kind = roofline_view(name, topo)
+    orc_frames = _oracle().workload_frames(name)
+    assert all(wx_state_bytes(st) == o[2] for st, o in zip(states, orc_frames)), "uniforms differ from the oracle's"
+    parts = {"sphere": 1, "noise": 32}[name]
+    rays_s, _, bpr, grazing = oracle_sample(view, orc_frames, 0, parts, os.cpu_count() or 1, seed=5, stats=True)
+    del view
+    peak, peak_kind = hbm_peak()
+    launch_ms = m / len(frames)
+    achieved = bpr * frames[0].rays / (launch_ms / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_kind": peak_kind, "kernel": kernel, "algorithmic_bytes_per_ray": bpr, "launch_ms": launch_ms,
+            "view": view_kind, "oracle_sample_rays": rays_s}
+    if name == "sphere":  # 2 MB of pools: L2-resident
+        l2 = l2_copy_peak(dev)
+        roof["l2"] = {"peak": l2, "frac": achieved / l2,
+                      "peak_kind": "measured here: device copy between two L2-resident 32 MiB buffers"}
+    return {"config": workload_config(name, (info["n5"], info["n4"], info["n3"]), info["active_voxels"],
+                                      [(f.width, f.height) for f in frames]),
+            "value": value, "unit": "Grays/s", "ms_per_step": m, "steps": steps, "warmup": warmup,
+            "grid_build_gpu_s": round(t_build, 3), "device_bytes": info["device_bytes"], "tuning": tn,
+            "autotune_best": tuned["best"], "roofline": roof, "grazing_fraction": grazing, "clocks": clk.summary()}
+
+
+def wx_state_bytes(st) -> bytes:
+    import woxel_gb300 as wx
+
+    return wx.state_bytes(st)
 
 
 def main():
@@ -463,6 +552,10 @@ def main():
     ap.add_argument("--serve-duration", type=float, default=5.0, help="seconds of arrivals per rate")
     ap.add_argument("--serve-slice", type=int, default=65536, help="tiles per launch")
     ap.add_argument("--serve-timeout", type=float, default=300.0)
+    ap.add_argument("--no-extras", dest="extras", action="store_false",
+                    help="skip the sphere, noise and serving figures of the default run")
+    ap.add_argument("--extra-serve-rates", default="200,1000,5000")
+    ap.add_argument("--extra-serve-duration", type=float, default=4.0)
     ap.add_argument("--kernel", default=None, choices=["persistent", "pixel"],
                     help="fix the kernel (default: the autotuner's choice)")
     ap.add_argument("--tile-width", type=int, default=None)
@@ -726,6 +819,18 @@ def main():
                                     "sample": f"1/{parts * 16} of the tiles ({r1} rays)"}
         del view
 
+    # The other benchmark configurations (the sphere, the noise grid, serving), one GPU only.
+    extras = None
+    if args.extras and world == 1 and args.workload == "spheres":
+        extras = {}
+        t0 = time.perf_counter()
+        for name in ("sphere", "noise"):
+            extras[name] = extra_workload(ctx, name, dev, flush, args.steps, args.warmup)
+            log(f"[bench] {name}: {extras[name]['value']:.3f} Grays/s, roofline {extras[name]['roofline']['frac']:.3f}")
+        extras["serving"] = serve_sweep(ctx, [float(x) for x in args.extra_serve_rates.split(",")],
+                                        args.extra_serve_duration)
+        extras["seconds"] = round(time.perf_counter() - t0, 1)
+
     if rank == 0:
         line = {
             "metric": "primary_ray_grays_per_s", "value": value, "unit": "Grays/s", "n_gpus": world,
@@ -742,6 +847,7 @@ def main():
                                            "seconds": tuned["seconds"]}},
             "frame_latency_ms": {"p50": p50, "p99": p99},
             "batched_same_frames": same_batched, "batched": batched, "shadow_rays": shadow, "surface": surface,
+            "other_configs": extras,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "grazing_rays": graze,
             "gpu_launches": len(frames) * args.steps,
             "clocks": clk.summary(),

@@ -117,17 +117,20 @@ def test_server_cancels_admitted_requests_mid_render(cuda_ctx):
     gid = srv.add_grid(grid)
     eyes = wx.orbit_eyes(8, 3000.0, 77)
     reqs = []
-    for i in range(8):  # 4K frames: the first four fill the first launch (about 1M tiles)
-        w, h = (3840, 2160) if i < 6 else (640, 480)
+    # 4K frames. The first submission starts a launch of its own; the next requests arrive
+    # while it runs and share the second launch (about 1M tiles: requests 1-4 and the start
+    # of 5), which runs for several milliseconds.
+    for i in range(8):
+        w, h = (3840, 2160) if i < 7 else (640, 480)
         st = wx.state_build(eye=tuple(float(x) for x in eyes[i]), target=(0, 0, 0), aspect=w / h, fovy=60.0,
                             width=float(w), mode=3)
         reqs.append(wx.Server.request(gid, st, w, h, user=i))
     tickets = [srv.submit(r) for r in reqs]
     t0 = time.time()
-    while srv.stats["launches"] < 1 and time.time() - t0 < 10:
+    while srv.stats["launches"] < 2 and time.time() - t0 < 10:
         pass
-    srv.cancel(tickets[3])  # last request of the running launch: its tiles come last in its queue
-    srv.cancel(tickets[5])  # in the next launch: dropped before it is launched
+    srv.cancel(tickets[4])  # last request of the running launch: its tiles come last in its queue
+    srv.cancel(tickets[6])  # in the next launch: dropped before it is launched
     got, t0 = [], time.time()
     while len(got) < 8 and time.time() - t0 < 60:
         got += srv.poll(16, wait_ms=20)
@@ -139,7 +142,7 @@ def test_server_cancels_admitted_requests_mid_render(cuda_ctx):
     with pytest.raises(wx.WxError):
         srv.cancel(tickets[0])  # finished
     for res in got:
-        if res.user in (3, 5):
+        if res.user in (4, 6):
             assert res.status == 7 and not res.rgba8  # WX_ERR_CANCELLED, no buffers
         else:
             assert res.status == 0
