@@ -165,23 +165,6 @@ __device__ __forceinline__ uint32_t leaf_overflow(const DevGrid &g, uint32_t key
     return lo < g.n_ovf ? __ldg(&g.ovf[lo].y) : 255u;
 }
 
-// Predicated loads through the read-only path: issued only when p holds (the
-// address need not be valid otherwise); the result is 0 when p is false.
-__device__ __forceinline__ uint32_t ldg_u32_if(bool p, const uint32_t *a) {
-    uint32_t v = 0u;
-    asm("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %2, 0;\n\t@q ld.global.nc.u32 %0, [%1];\n\t}"
-        : "+r"(v)
-        : "l"(a), "r"((uint32_t)p));
-    return v;
-}
-__device__ __forceinline__ uint32_t ldg_u8_if(bool p, const uint8_t *a) {
-    uint32_t v = 0u;
-    asm("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %2, 0;\n\t@q ld.global.nc.u8 %0, [%1];\n\t}"
-        : "+r"(v)
-        : "l"(a), "r"((uint32_t)p));
-    return v;
-}
-
 constexpr uint32_t kNoNode = 0xFFFFFFFFu;
 
 // Index of the N5 whose origin is (x, y, z) & ~4095, or kNoNode: the dense
@@ -219,61 +202,61 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     const int x = __float2int_rd(r.px), y = __float2int_rd(r.py), z = __float2int_rd(r.pz);
     const uint32_t d = (uint32_t)((x ^ r.lx) | (y ^ r.ly) | (z ^ r.lz));
     r.lx = x; r.ly = y; r.lz = z;
-    // The deepest cached node that still contains the voxel (:360-396): the
-    // previous voxel lies in every cached node, so the voxel is in the cached
-    // node of side 8, 128 or 4096 when d is below that side. c counts those
-    // sides, and the cached chain is valid down to min(np, c) levels:
-    // 3 -> the leaf, 2 -> the N4, 1 -> the N5, 0 -> a root lookup.
-    const uint32_t c = (d < 8u ? 1u : 0u) + (d < 128u ? 1u : 0u) + (d < 4096u ? 1u : 0u);
-    const uint32_t valid = min(r.np, c);
-    uint32_t lvl = valid ? 6u - valid : 0u;  // level resolved next: 3, 4, 5, or 0 (root)
-    if (lvl == 0u) {  // get_vdb_leaf_from_nothing (:398-413): the N5 whose origin is floor(p) & ~4095
+    int lvl;
+    if (r.np == 3 && d < 8u) lvl = 3;
+    else if (r.np >= 2 && d < 128u) lvl = 4;
+    else if (r.np >= 1 && d < 4096u) lvl = 5;
+    else lvl = 0;
+    uint32_t dist = 1;
+    // 2^sk and 2^-sk as float bits, sk = log2 of the size scale of the level
+    // that resolves the voxel (:105-112): 12, 7, 3, 0 for 0..3 cached parents.
+    uint32_t sbits = (127u + 12u) << 23, rbits = (127u - 12u) << 23;
+    if (lvl == 0) {  // get_vdb_leaf_from_nothing (:398-413): the N5 whose origin is floor(p) & ~4095
+        r.np = 0;
         const uint32_t k = root_find(g, x, y, z);
         if (k != kNoNode) {
             r.i5 = k;
-            lvl = 5u;
+            lvl = 5;
         }
     }
-    // The three levels as predicated straight-line code: a lane loads the slot
-    // word (or leaf byte) of the level it resolves and skips the others. The
-    // decision at each level is the shader's: a child descends; otherwise the
-    // word is the skip distance (0 = an active tile or voxel = a hit).
-    uint32_t dist = 1u;  // a root miss skips one N5 (:404-412)
-    {  // get_vdb_leaf_from_node5 (:415-444)
-        const bool s5 = lvl == 5u;
-        if (s5 && !wx_in_range(r.i5, g.n5)) return 1u;
+    if (lvl == 5) {  // get_vdb_leaf_from_node5 (:415-444)
+        if (!wx_in_range(r.i5, g.n5)) return 1u;
         const uint32_t off = ((((uint32_t)x >> 7) & 31u) << 10) | ((((uint32_t)y >> 7) & 31u) << 5) |
                              (((uint32_t)z >> 7) & 31u);
-        const uint32_t w = ldg_u32_if(s5, g.slot5 + ((r.i5 << 15) | off));
-        const bool child = (w & kChild) != 0u;
-        if (s5 && child) r.i4 = w & ~kChild;
-        if (s5 && !child) dist = w;
-        if (child) lvl = 4u;  // w is 0 unless s5
+        const uint32_t w = __ldg(g.slot5 + ((r.i5 << 15) | off));
+        r.np = 1;
+        sbits = (127u + 7u) << 23;
+        rbits = (127u - 7u) << 23;
+        if (w & kChild) {
+            r.i4 = w & ~kChild;
+            lvl = 4;
+        } else {
+            dist = w;
+        }
     }
-    {  // get_vdb_leaf_from_node4 (:446-475)
-        const bool s4 = lvl == 4u;
-        if (s4 && !wx_in_range(r.i4, g.n4)) return 1u;
+    if (lvl == 4) {  // get_vdb_leaf_from_node4 (:446-475)
+        if (!wx_in_range(r.i4, g.n4)) return 1u;
         const uint32_t off = ((((uint32_t)x >> 3) & 15u) << 8) | ((((uint32_t)y >> 3) & 15u) << 4) |
                              (((uint32_t)z >> 3) & 15u);
-        const uint32_t w = ldg_u32_if(s4, g.slot4 + ((r.i4 << 12) | off));
-        const bool child = (w & kChild) != 0u;
-        if (s4 && child) r.i3 = w & ~kChild;
-        if (s4 && !child) dist = w;
-        if (child) lvl = 3u;
+        const uint32_t w = __ldg(g.slot4 + ((r.i4 << 12) | off));
+        r.np = 2;
+        sbits = (127u + 3u) << 23;
+        rbits = (127u - 3u) << 23;
+        if (w & kChild) {
+            r.i3 = w & ~kChild;
+            lvl = 3;
+        } else {
+            dist = w;
+        }
     }
-    {  // get_vdb_leaf_from_node3 (:477-494)
-        const bool s3 = lvl == 3u;
-        if (s3 && !wx_in_range(r.i3, g.n3)) return 1u;
+    if (lvl == 3) {  // get_vdb_leaf_from_node3 (:477-494)
+        if (!wx_in_range(r.i3, g.n3)) return 1u;
         const uint32_t key = (r.i3 << 9) | (((uint32_t)x & 7u) << 6) | (((uint32_t)y & 7u) << 3) | ((uint32_t)z & 7u);
-        const uint32_t b = ldg_u8_if(s3, g.leaf + key);
-        if (s3) dist = b;
-        if (s3 && b == 255u) dist = leaf_overflow(g, key);
+        dist = __ldg(g.leaf + key);
+        if (dist == 255u) dist = leaf_overflow(g, key);
+        r.np = 3;
+        sbits = rbits = 127u << 23;
     }
-    // Levels reached: 5 -> one cached parent, 4 -> two, 3 -> three, a root miss none;
-    // the size scale of the resolving level (:105-112) is 2^sk, sk = 12, 7, 3, 0 by np.
-    r.np = lvl ? 6u - lvl : 0u;
-    const uint32_t sk = (0x0003070Cu >> (8u * r.np)) & 0xFFu;
-    const uint32_t sbits = (127u + sk) << 23, rbits = (127u - sk) << 23;
     if (dist == 0u) return 0u;
     const float apx = fabsf(r.px), apy = fabsf(r.py), apz = fabsf(r.pz);
     // any(4096 < |p|); a NaN coordinate compares false, and fmaxf skips NaN.
