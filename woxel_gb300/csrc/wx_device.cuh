@@ -270,7 +270,12 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     bool fast;
     const float ys = rcp_size(dist, rbits, &fast);
     // tMax = idir * (size * step01 - (p - size * floor(p / size)))  (:78-80, :114)
-    const float ax = r.dx < 0.0f ? 0.0f : 1.0f, ay = r.dy < 0.0f ? 0.0f : 1.0f, az = r.dz < 0.0f ? 0.0f : 1.0f;
+    // step01 = max(0, sign11(dir)): 0 where dir < 0, else 1. The fast step only
+    // takes rays whose direction components are nonzero numbers, for which
+    // copysign(0.5, d) + 0.5 gives the same 0 or 1 (on the FMA pipe).
+    const float ax = kCareful ? (r.dx < 0.0f ? 0.0f : 1.0f) : __fadd_rn(copysignf(0.5f, r.dx), 0.5f);
+    const float ay = kCareful ? (r.dy < 0.0f ? 0.0f : 1.0f) : __fadd_rn(copysignf(0.5f, r.dy), 0.5f);
+    const float az = kCareful ? (r.dz < 0.0f ? 0.0f : 1.0f) : __fadd_rn(copysignf(0.5f, r.dz), 0.5f);
     float tx, ty, tz;
     // The fast quotient needs every coordinate of magnitude >= 2^-64 (a zero
     // coordinate also takes the IEEE path here; both give the same floor).
