@@ -44,7 +44,7 @@ __device__ __forceinline__ bool tile_pixel(const Job &J, uint32_t tl, uint32_t l
     return gx < (J.width & ~7u) && gy < (J.height & ~3u);
 }
 
-template <bool kAll>
+template <bool kAll, bool kFmaStep01 = true>
 __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t lane, bool wait_prev) {
     uint32_t gx, gy;
     // The warp's lanes leave each march at different iterations. Without the
@@ -56,7 +56,7 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
     const wx_state_uniform &s = J.s;
     const F3 dir = primary_dir(s, gx, gy);
     const F3 eye = f3(s.eye[0], s.eye[1], s.eye[2]);
-    const March hit = hdda(J.g, eye, dir);
+    const March hit = hdda<kFmaStep01>(J.g, eye, dir);
     __syncwarp(act);
     F3 c;
     uint32_t shadow = 0, reserved = 0;
@@ -87,7 +87,7 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
         c = primary_colour(s, hit, dir, &need, &shadowed, &src);
         __syncwarp(act);  // shadow rays of the warp start together
         if (need) {
-            const March sh = hdda(J.g, src, -f3(s.sun_dir[0], s.sun_dir[1], s.sun_dir[2]));
+            const March sh = hdda<kFmaStep01>(J.g, src, -f3(s.sun_dir[0], s.sun_dir[1], s.sun_dir[2]));
             shadow = 1u | (sh.state << 1) | (sh.i << 8);
             if (sh.state == 0u) c = shadowed;
         }
@@ -384,9 +384,9 @@ __global__ void WX_RAY_BOUNDS k_persistent(const Job *__restrict__ jobs, uint32_
                     continue;
                 }
             }
-            render_pixel<kAll>(J, t - J.tile_begin + J.tile_off, lane, true);
+            render_pixel<kAll, false>(J, t - J.tile_begin + J.tile_off, lane, true);
         } else {
-            render_pixel<kAll>(job0, t, lane, true);
+            render_pixel<kAll, false>(job0, t, lane, true);
         }
     }
 }

@@ -195,7 +195,7 @@ __device__ __forceinline__ uint32_t root_find(const DevGrid &g, int x, int y, in
 // r.i is the iteration count the shader reports. kCareful selects the
 // NaN-aware min/argmin and the literal nudge (see ray_needs_careful_step);
 // both variants give identical results on the rays the fast one is used for.
-template <bool kCareful>
+template <bool kCareful, bool kFmaStep01 = true>
 __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     if (r.i >= kMaxSteps) return 2u;
     // vec3<i32>(floor(p)): one saturating round-down conversion (NaN -> 0).
@@ -273,9 +273,13 @@ __device__ __forceinline__ uint32_t ray_step(const DevGrid &g, Ray &r) {
     // step01 = max(0, sign11(dir)): 0 where dir < 0, else 1. The fast step only
     // takes rays whose direction components are nonzero numbers, for which
     // copysign(0.5, d) + 0.5 gives the same 0 or 1 (on the FMA pipe).
-    const float ax = kCareful ? (r.dx < 0.0f ? 0.0f : 1.0f) : __fadd_rn(copysignf(0.5f, r.dx), 0.5f);
-    const float ay = kCareful ? (r.dy < 0.0f ? 0.0f : 1.0f) : __fadd_rn(copysignf(0.5f, r.dy), 0.5f);
-    const float az = kCareful ? (r.dz < 0.0f ? 0.0f : 1.0f) : __fadd_rn(copysignf(0.5f, r.dz), 0.5f);
+    // kFmaStep01 = false keeps the compare-and-select form in the fast step too:
+    // the persistent kernels spill more with the copysign form and run slower
+    // with it (4.45 -> 4.32 Grays/s on the mixed batch), while k_pixel gains.
+    constexpr bool kSel = kCareful || !kFmaStep01;
+    const float ax = kSel ? (r.dx < 0.0f ? 0.0f : 1.0f) : __fadd_rn(copysignf(0.5f, r.dx), 0.5f);
+    const float ay = kSel ? (r.dy < 0.0f ? 0.0f : 1.0f) : __fadd_rn(copysignf(0.5f, r.dy), 0.5f);
+    const float az = kSel ? (r.dz < 0.0f ? 0.0f : 1.0f) : __fadd_rn(copysignf(0.5f, r.dz), 0.5f);
     float tx, ty, tz;
     // The fast quotient needs every coordinate of magnitude >= 2^-64 (a zero
     // coordinate also takes the IEEE path here; both give the same floor).
@@ -365,15 +369,16 @@ __device__ __forceinline__ March march_result(const Ray &r, uint32_t st) {
 }
 
 // hdda_ray (raycast.comp.wgsl:84-126) run to completion.
+template <bool kFmaStep01 = true>
 __device__ __forceinline__ March hdda(const DevGrid &g, F3 src, F3 dir) {
     Ray r;
     ray_init(r, src, dir);
     uint32_t st;
     if (ray_needs_careful_step(src, dir)) {
-        while ((st = ray_step<true>(g, r)) == 0xFFu) {
+        while ((st = ray_step<true, kFmaStep01>(g, r)) == 0xFFu) {
         }
     } else {
-        while ((st = ray_step<false>(g, r)) == 0xFFu) {
+        while ((st = ray_step<false, kFmaStep01>(g, r)) == 0xFFu) {
         }
     }
     return march_result(r, st);
