@@ -81,6 +81,33 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
             F3 shadowed, src;
             c = primary_colour(s, hit, dir, &need, &shadowed, &src);  // states 1, 2: mode 3's colours
         }
+    } else if (!kFmaStep01) {  // modes 0-3 in the persistent kernels
+        // Everything the stores need is reduced to a few words before the shadow
+        // march (the packed colour, t, the info word), so that the direction and
+        // both candidate colours are not live across it: the persistent kernels
+        // then spill 32 bytes instead of 92 and the mixed batch runs at 4.80
+        // instead of 4.58 Grays/s (k_pixel, with fewer registers, gains nothing).
+        bool need;
+        F3 shadowed, src;
+        const F3 cc = primary_colour(s, hit, dir, &need, &shadowed, &src);
+        uint32_t cpk = pack_rgba(cc);
+        const float t = dot3(hit.p - eye, dir);
+        const uint32_t info = hit.state | (hit.np << 2) | (hit.mask << 4) | (hit.i << 8);
+        const F3 hp = hit.p;
+        const uint32_t node = hit.node;
+        __syncwarp(act);  // shadow rays of the warp start together
+        if (need) {
+            const March sh = hdda<kFmaStep01>(J.g, src, -f3(s.sun_dir[0], s.sun_dir[1], s.sun_dir[2]));
+            shadow = 1u | (sh.state << 1) | (sh.i << 8);
+            if (sh.state == 0u) cpk = pack_rgba(ambient_colour());  // shadowed is I_a
+        }
+        __syncwarp(act);
+        const uint32_t pix = gy * J.width + gx;
+        if (wait_prev) asm volatile("griddepcontrol.wait;" ::: "memory");
+        if (!wx_in_range(pix, (uint64_t)J.width * J.height)) return;
+        J.rgba[pix] = cpk;
+        if (J.hits) store_hit(J.hits + pix, hp, t, node, info, shadow, 0u);
+        return;
     } else {  // modes 0-3: every valid lane of the warp comes here (the __syncwarp below needs them all)
         bool need;
         F3 shadowed, src;
