@@ -9,9 +9,8 @@ generator, SDF, pools and kernels.
   oracle-built view; batched launch == per-frame launches; repeated renders identical.
 * noise grid, 3840x2160, mode 0 (first active voxel): the [-2048,0)^3 octant of the
   benchmark's 4096^3 grid (367,660 leaves) against the oracle-built view of that octant;
-  and the whole 2.68M-leaf grid against the oracle marching over the product's flattened
-  view (the march at full size; the SDF of the whole grid takes the single-threaded oracle
-  minutes, so the octant carries the independent SDF check).
+  and the whole 2.68M-leaf grid (GPU SDF build) against the oracle's own view of it, built
+  on a host thread while the other GPU tests run.
 """
 import numpy as np
 import pytest
@@ -122,15 +121,19 @@ def test_noise_octant_4k_sampled_tiles(cuda_ctx):
     assert hits > 10000
 
 
-def test_noise_4k_sampled_tiles(cuda_ctx):
+def test_noise_4k_sampled_tiles(cuda_ctx, oracle_noise_view):
+    """The whole noise grid: product generator, GPU SDF build and pools against the oracle's
+    generator, compute_sdf and atlas() (built on a host thread while the other tests ran)."""
     topo = W.noise_topology()
     n5, n4, n3 = topo.counts
     assert abs(n3 / (512 ** 3) - 0.02) < 0.001  # 2.0% of the 8^3 leaf lattice
-    grid = cuda_ctx.build_grid(topo)
+    grid = cuda_ctx.build_grid(topo, gpu=True)
     assert grid.info["n3"] == n3
-    view = topo.view()
+    view = oracle_noise_view
+    assert view["vals3"].size // 16 == n3
     frame = W.noise_frames()[0]
-    rg, hg = sampled_parity(cuda_ctx, grid, view, frame, ntiles=600, seed=3)
+    ostate = orc.workload_frames("noise")[0][2]
+    rg, hg = sampled_parity(cuda_ctx, grid, view, frame, ntiles=600, seed=3, oracle_state=ostate)
     f = wx.hit_fields(hg)
     hit = f["state"] == 0
     assert hit.mean() > 0.05 and (f["level"][hit] == 3).all()  # first active voxel, always inside a leaf
