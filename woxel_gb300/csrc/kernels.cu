@@ -137,10 +137,11 @@ __device__ __forceinline__ void render_pixel(const Job &J, uint32_t tl, uint32_t
 // 48 registers a thread and 40 resident warps per SM. k_pixel: at least 6, 40
 // registers and 48 warps (modes 0-3; the kernel of every mode keeps 48 registers,
 // which its glossy and zero-crossing code needs). Measured on GB300 (16 frames of 2000 spheres at
-// 1080p): k_pixel 3.17 Grays/s at 40 registers against 3.03 at 48 (its finished
-// blocks retire while the previous frame ends, so more resident warps pay); the
-// persistent kernels lose 6-8% at 40 registers (spills in the march loop) and
-// beat 64 (32 warps) by 2% and 80 (24 warps) by 17% at 48.
+// 1080p): k_pixel 3.34 Grays/s at 40 registers against 3.17 at 48 and 3.30 at 32
+// (its finished blocks retire while the previous frame ends, so more resident warps
+// pay); the persistent kernels are slower at 40 registers (the mixed batch 4.38
+// against 4.80 Grays/s at 48; spills in the march loop) and beat 64 (32 warps) by 2%
+// and 80 (24 warps) by 17% at 48.
 #define WX_RAY_BOUNDS __launch_bounds__(256, 5)
 #define WX_PIXEL_BOUNDS __launch_bounds__(256, kAll ? 5 : 6)
 
