@@ -83,7 +83,7 @@ def replica_throughput(rays_per_rank: int, world: int, ms: float) -> float:
 # capture of the benchmark's kernel on each workload, with the commit it was taken on.
 # Reported as roofline.traffic_from_profile: a recorded capture, not a figure of this run.
 NCU_TRAFFIC = {
-    ("k_pixel", "spheres"): (142547456, "1d05970"),
+    ("k_pixel", "spheres"): (142257408, "5c05830"),
 }
 
 
