@@ -88,33 +88,90 @@ NCU_TRAFFIC = {
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle samples during the timed region."""
+    """SM clock and throttle-reason samples during the timed region, from two sources:
+    `nvidia-smi -lms 200` (the process is started, and its first sample awaited, before
+    the region begins) and NVML itself, polled every 10 ms from a thread through ctypes
+    (libnvidia-ml: nvmlDeviceGetClockInfo / nvmlDeviceGetCurrentClocksEventReasons, read
+    only), which gives tens of samples even in a sub-second region."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason bits (nvml.h)
+    NVML_REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+                    0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
-    def __init__(self, device: int):
+    def __init__(self, device: int, period_s: float = 0.01):
         self.device = device
+        self.period = period_s
         self.proc = None
         self.lines = []
+        self.first = threading.Event()
+        self.nv = []          # (sm MHz, reason bits)
+        self.nv_max = None
+        self.stop = threading.Event()
+        self.nt = None
+
+    def _nvml_index(self) -> int:
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        ids = [v.strip() for v in vis.split(",") if v.strip()]
+        if ids and all(v.isdigit() for v in ids) and self.device < len(ids):
+            return int(ids[self.device])
+        return self.device
+
+    def _nvml_start(self):
+        import ctypes as C
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return
+        h = C.c_void_p()
+        if lib.nvmlInit_v2() != 0 or lib.nvmlDeviceGetHandleByIndex_v2(self._nvml_index(), C.byref(h)) != 0:
+            return
+        get_reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons", None)
+        mx = C.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0:  # NVML_CLOCK_SM
+            self.nv_max = float(mx.value)
+
+        def poll():
+            clk, rs = C.c_uint(), C.c_ulonglong()
+            while not self.stop.is_set():
+                if lib.nvmlDeviceGetClockInfo(h, 1, C.byref(clk)) == 0:
+                    bits = rs.value if get_reasons is not None and get_reasons(h, C.byref(rs)) == 0 else 0
+                    self.nv.append((float(clk.value), int(bits)))
+                self.stop.wait(self.period)
+
+        self.nt = threading.Thread(target=poll, daemon=True)
+        self.nt.start()
 
     def __enter__(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self._nvml_index()), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self.first.wait(5.0)
         except FileNotFoundError:
             self.proc = None
+        self._nvml_start()
+        if self.nt is not None:
+            t0 = time.time()
+            while not self.nv and time.time() - t0 < 1.0:
+                time.sleep(0.001)
+            del self.nv[:]   # samples from the timed region only
         return self
 
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+            self.first.set()
 
     def __exit__(self, *exc):
+        self.stop.set()
+        if self.nt is not None:
+            self.nt.join(timeout=2)
         if self.proc:
             self.proc.terminate()
             try:
@@ -137,8 +194,18 @@ class ClockSampler:
             for n, v in zip(names, f[5:9]):
                 if v.lower() == "active":
                     reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+               "samples": len(sm), "source": "nvidia-smi -lms 200"}
+        if self.nv:
+            nv_sm = [c for c, _ in self.nv]
+            for _, bits in self.nv:
+                reasons.update(n for b, n in self.NVML_REASONS.items() if bits & b)
+            out.update({"sm_mhz": statistics.median(nv_sm), "sm_min_mhz": min(nv_sm),
+                        "sm_max_mhz": self.nv_max if self.nv_max is not None else smax,
+                        "reasons": sorted(reasons), "samples": len(nv_sm),
+                        "source": "NVML every 10 ms; nvidia-smi -lms 200",
+                        "nvidia_smi": {"sm_mhz": out["sm_mhz"], "samples": len(sm)}})
+        return out
 
 
 # --------------------------------------------------------------------------
