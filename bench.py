@@ -111,6 +111,8 @@ class ClockSampler:
         self.nv_max = None
         self.stop = threading.Event()
         self.nt = None
+        self.sample = None
+        self.bracket = []     # one sample just before and one just after the region
 
     def _nvml_index(self) -> int:
         vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
@@ -134,14 +136,21 @@ class ClockSampler:
         if lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0:  # NVML_CLOCK_SM
             self.nv_max = float(mx.value)
 
-        def poll():
+        def sample():
             clk, rs = C.c_uint(), C.c_ulonglong()
+            if lib.nvmlDeviceGetClockInfo(h, 1, C.byref(clk)) != 0:
+                return None
+            bits = rs.value if get_reasons is not None and get_reasons(h, C.byref(rs)) == 0 else 0
+            return float(clk.value), int(bits)
+
+        def poll():
             while not self.stop.is_set():
-                if lib.nvmlDeviceGetClockInfo(h, 1, C.byref(clk)) == 0:
-                    bits = rs.value if get_reasons is not None and get_reasons(h, C.byref(rs)) == 0 else 0
-                    self.nv.append((float(clk.value), int(bits)))
+                v = sample()
+                if v is not None:
+                    self.nv.append(v)
                 self.stop.wait(self.period)
 
+        self.sample = sample
         self.nt = threading.Thread(target=poll, daemon=True)
         self.nt.start()
 
@@ -161,6 +170,8 @@ class ClockSampler:
             while not self.nv and time.time() - t0 < 1.0:
                 time.sleep(0.001)
             del self.nv[:]   # samples from the timed region only
+        if self.sample is not None:
+            self.bracket.append(self.sample())
         return self
 
     def _read(self):
@@ -169,6 +180,8 @@ class ClockSampler:
             self.first.set()
 
     def __exit__(self, *exc):
+        if self.sample is not None:
+            self.bracket.append(self.sample())
         self.stop.set()
         if self.nt is not None:
             self.nt.join(timeout=2)
@@ -196,14 +209,19 @@ class ClockSampler:
                     reasons.add(n)
         out = {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
                "samples": len(sm), "source": "nvidia-smi -lms 200"}
-        if self.nv:
-            nv_sm = [c for c, _ in self.nv]
-            for _, bits in self.nv:
+        nv = self.nv
+        src = "NVML every 10 ms; nvidia-smi -lms 200"
+        if not nv:  # a region shorter than the sampling period
+            nv = [b for b in self.bracket if b is not None]
+            src = "NVML just before and just after the timed region (shorter than 10 ms)"
+        if nv:
+            nv_sm = [c for c, _ in nv]
+            for _, bits in nv:
                 reasons.update(n for b, n in self.NVML_REASONS.items() if bits & b)
             out.update({"sm_mhz": statistics.median(nv_sm), "sm_min_mhz": min(nv_sm),
                         "sm_max_mhz": self.nv_max if self.nv_max is not None else smax,
                         "reasons": sorted(reasons), "samples": len(nv_sm),
-                        "source": "NVML every 10 ms; nvidia-smi -lms 200",
+                        "source": src,
                         "nvidia_smi": {"sm_mhz": out["sm_mhz"], "samples": len(sm)}})
         return out
 

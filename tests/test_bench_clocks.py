@@ -29,3 +29,12 @@ def test_nvml_index_follows_visible_devices(monkeypatch):
     assert bench.ClockSampler(1)._nvml_index() == 3
     monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "GPU-abc")
     assert bench.ClockSampler(1)._nvml_index() == 1
+
+
+def test_short_region_falls_back_to_bracketing_samples():
+    c = bench.ClockSampler(0)
+    c.lines = ["0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active"]
+    c.bracket = [(2070.0, 0), (2055.0, 0x20)]
+    s = c.summary()
+    assert s["samples"] == 2 and s["sm_mhz"] == 2062.5 and s["reasons"] == ["sw_thermal_slowdown"]
+    assert "before and just after" in s["source"]
