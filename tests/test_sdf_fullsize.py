@@ -28,8 +28,8 @@ def assert_views_equal(ov: dict, pv: dict):
         assert bad.size == 0, f"atlas {i}: {bad.size} words differ, first at {bad[:5]}"
 
 
-def test_spheres_grid_sdf_oracle_equals_product():
-    ov = orc.workload_view("spheres")
+def test_spheres_grid_sdf_oracle_equals_product(oracle_spheres_view):
+    ov = oracle_spheres_view
     pv = W.spheres_topology().view()
     assert ov["dims"][2][0] == 632
     assert_views_equal(ov, pv)
