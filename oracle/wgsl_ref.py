@@ -811,7 +811,17 @@ class Emitter:
             "    for (auto &x : th) x.join();\n"
             "    return 0;\n}\n\n"
             f'extern "C" void wref_workgroup_size(uint32_t *out) {{ out[0] = {wg[0]}; out[1] = {wg[1]}; out[2] = {wg[2]}; }}\n'
+            f'extern "C" const char *wref_bindings(void) {{ return "{self.binding_table()}"; }}\n'
         )
+
+    def binding_table(self):
+        """name:group:binding:kind;... of the shader's resources."""
+        rows = []
+        for g in self.m.globals:
+            _, name, ty, space, at, init = g
+            kind = space[0] if space else ty[1]
+            rows.append(f"{name}:{int(at['group'][0][1].rstrip('iu'))}:{int(at['binding'][0][1].rstrip('iu'))}:{kind}")
+        return ";".join(rows)
 
 
 def translate(src: str, entry: str = "cp_main") -> tuple:
@@ -854,7 +864,11 @@ class Shader:
         wg = (C.c_uint32 * 3)()
         self.lib.wref_workgroup_size(wg)
         self.wg = tuple(wg)
-        self.table = translate(shader_path().read_text())[1] if shader_path().exists() else None
+        self.lib.wref_bindings.restype = C.c_char_p
+        self.table = {}
+        for row in self.lib.wref_bindings().decode().split(";"):
+            name, g, b, kind = row.split(":")
+            self.table[name] = (int(g), int(b), kind)
 
     def render(self, view: dict, state: bytes, width: int, height: int, nthreads: int = 8):
         """RGBA8 (height, width, 4) of the dispatch wgpu issues for a width x height frame
