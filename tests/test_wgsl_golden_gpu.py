@@ -54,3 +54,35 @@ def test_kernels_match_reference_shader(golden, cuda_ctx, grids, kernel):
 
 def test_kernels_with_hit_records_match_reference_shader(golden, cuda_ctx, grids):
     _check(golden, cuda_ctx, grids, hits=True)
+
+
+def test_batched_launch_matches_reference_shader(golden, cuda_ctx, grids):
+    """All 66 frames over the five grids in one batched launch (the persistent kernel over
+    a job table, the path of wx_batch_* plans and the server), and again as a CUDA-graph
+    plan replayed twice."""
+    import torch
+
+    meta = golden["meta"]
+    outs, frames = [], []
+    for i, (g, w, h, large) in enumerate(meta):
+        st = wx.state_from_bytes(bytes(golden[f"state_{i}"]))
+        o = torch.zeros(int(w) * int(h) * 4, dtype=torch.uint8, device="cuda")
+        outs.append(o)
+        frames.append((grids[int(g)], st, int(w), int(h), o, None))
+    stream = torch.cuda.current_stream().cuda_stream
+    cuda_ctx.render_batch(frames, stream=stream)
+    torch.cuda.synchronize()
+
+    def check_all():
+        for i, (g, w, h, large) in enumerate(meta):
+            got = outs[i].cpu().numpy().reshape(int(h), int(w), 4)
+            assert np.array_equal(got, golden[f"rgba_{i}"]), f"frame {i} (grid {g}, {w}x{h})"
+
+    check_all()
+    plan = cuda_ctx.batch(frames)
+    for _ in range(2):
+        for o in outs:
+            o.zero_()
+        plan.launch(stream=stream)
+        torch.cuda.synchronize()
+        check_all()
