@@ -126,9 +126,9 @@ fn main(@builtin(global_invocation_id) gid: vec3<u32>) {
 """
     cpp, table = wgsl_ref.translate(src, entry="main")
     assert table == {"out_tex": (0, 0, "texture_storage_2d")}
-    (tmp_path / "s.wgsl").write_text(src)
-    so = tmp_path / "lib.so"
     import subprocess
+
+    so = tmp_path / "lib.so"
     cpp_file = tmp_path / "s.cpp"
     cpp_file.write_text(cpp)
     subprocess.run(["g++", "-O1", "-std=c++20", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
