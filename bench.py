@@ -112,6 +112,7 @@ class ClockSampler:
         self.stop = threading.Event()
         self.nt = None
         self.sample = None
+        self.nvml_shutdown = None
         self.bracket = []     # one sample just before and one just after the region
 
     def _nvml_index(self) -> int:
@@ -151,6 +152,7 @@ class ClockSampler:
                 self.stop.wait(self.period)
 
         self.sample = sample
+        self.nvml_shutdown = lib.nvmlShutdown
         self.nt = threading.Thread(target=poll, daemon=True)
         self.nt.start()
 
@@ -185,6 +187,7 @@ class ClockSampler:
         self.stop.set()
         if self.nt is not None:
             self.nt.join(timeout=2)
+            self.nvml_shutdown()  # balances this sampler's nvmlInit_v2
         if self.proc:
             self.proc.terminate()
             try:
