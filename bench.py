@@ -452,7 +452,7 @@ def measure_mixed(ctx, grids, dev, flush, steps, warmup):
     }
 
 
-def serve_sweep(ctx, rates, duration, slice_tiles=65536, timeout=300.0):
+def serve_sweep(ctx, rates, duration, slice_tiles=262144, timeout=300.0):
     """Serving: open-loop Poisson arrivals over 8 resident grids (4 sphere-generator grids with
     distinct seeds, 4 2000-sphere grids with seeds 2..5, built on the GPU), the resolution mix
     of the mixed requests, HBM budget 150 GB. Each rate is replayed on the continuous-batching
@@ -638,7 +638,7 @@ def main():
     ap.add_argument("--serve", action="store_true", help="run the serving sweep (Poisson arrivals over 8 grids) instead")
     ap.add_argument("--serve-rates", default="100,200,500,1000,2000,5000")
     ap.add_argument("--serve-duration", type=float, default=5.0, help="seconds of arrivals per rate")
-    ap.add_argument("--serve-slice", type=int, default=65536, help="tiles per launch")
+    ap.add_argument("--serve-slice", type=int, default=262144, help="tiles per launch")
     ap.add_argument("--serve-timeout", type=float, default=300.0)
     ap.add_argument("--no-extras", dest="extras", action="store_false",
                     help="skip the sphere, noise and serving figures of the default run")

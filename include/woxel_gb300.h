@@ -290,7 +290,7 @@ typedef struct wx_server wx_server;
 typedef struct wx_server_config {
     uint64_t budget_bytes;  /* HBM budget: resident grids + the output arena */
     uint32_t max_inflight;  /* launches in flight, 1..8 (default 2) */
-    uint32_t slice_tiles;   /* tiles per launch; 0 = 65536 (one 1080p frame) */
+    uint32_t slice_tiles;   /* tiles per launch; 0 = 262144 (four 1080p frames) */
     uint32_t max_frames;    /* request pieces per launch, 1..1024 (default 256) */
     uint32_t flags;         /* WX_SERVE_FIFO */
 } wx_server_config;

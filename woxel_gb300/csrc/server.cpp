@@ -306,7 +306,10 @@ int wx_server_create(wx_ctx *ctx, const wx_server_config *cfg, wx_server **out) 
     if (!ctx || !cfg || !out) return sfail(WX_ERR_INVALID, "wx_server_create: null argument");
     wx_server_config c = *cfg;
     if (c.max_inflight == 0) c.max_inflight = 2;
-    if (c.slice_tiles == 0) c.slice_tiles = 65536;
+    // Default slice: four 1080p frames. Measured at saturation (5000 req/s over the 8
+    // benchmark grids): 3.58 Grays/s at 16,384 tiles per launch, 5.62 at 65,536, 5.90 at
+    // 262,144 and 5.94 at 1,048,576, with p50/p99 at 200-2000 req/s unchanged or better.
+    if (c.slice_tiles == 0) c.slice_tiles = 262144;
     if (c.max_frames == 0) c.max_frames = 256;
     if (c.max_inflight > 8 || c.max_frames > 1024)
         return sfail(WX_ERR_INVALID, "wx_server_create: max_inflight must be <= 8 and max_frames <= 1024");
