@@ -452,7 +452,7 @@ def measure_mixed(ctx, grids, dev, flush, steps, warmup):
     }
 
 
-def serve_sweep(ctx, rates, duration, slice_tiles=262144, timeout=300.0):
+def serve_sweep(ctx, rates, duration, slice_tiles=262144, timeout=300.0, max_inflight=2):
     """Serving: open-loop Poisson arrivals over 8 resident grids (4 sphere-generator grids with
     distinct seeds, 4 2000-sphere grids with seeds 2..5, built on the GPU), the resolution mix
     of the mixed requests, HBM budget 150 GB. Each rate is replayed on the continuous-batching
@@ -491,7 +491,8 @@ def serve_sweep(ctx, rates, duration, slice_tiles=262144, timeout=300.0):
 
     out = []
     for mode in ("batched", "fifo"):
-        srv = wx.Server(ctx, budget_bytes=budget, max_inflight=2, slice_tiles=slice_tiles, fifo=(mode == "fifo"))
+        srv = wx.Server(ctx, budget_bytes=budget, max_inflight=max_inflight, slice_tiles=slice_tiles,
+                        fifo=(mode == "fifo"))
         for g in grids:
             srv.add_grid(g)
         wreqs, _, _ = trace(50.0, 1)  # warm-up: a few requests
@@ -521,7 +522,7 @@ def serve_sweep(ctx, rates, duration, slice_tiles=262144, timeout=300.0):
             "value": best["served_grays_per_s"], "fifo_value": fifo_best["served_grays_per_s"], "unit": "Grays/s",
             "speedup_over_fifo": best["served_grays_per_s"] / fifo_best["served_grays_per_s"],
             "budget_bytes": budget, "grid_bytes": grid_bytes, "duration_s_per_rate": duration,
-            "slice_tiles": slice_tiles, "max_inflight": 2, "sweep": out}
+            "slice_tiles": slice_tiles, "max_inflight": max_inflight, "sweep": out}
 
 
 def run_serve(args):
@@ -533,7 +534,7 @@ def run_serve(args):
     torch.cuda.set_device(0)
     ctx = wx.Context(0)
     r = serve_sweep(ctx, [float(x) for x in args.serve_rates.split(",")], args.serve_duration, args.serve_slice,
-                    args.serve_timeout)
+                    args.serve_timeout, args.serve_inflight)
     print(json.dumps({"metric": "served_primary_ray_grays_per_s", "value": r.pop("value"), "unit": "Grays/s",
                       "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
                       "config": {"workload": r.pop("workload")}, **r}), flush=True)
@@ -639,6 +640,7 @@ def main():
     ap.add_argument("--serve-rates", default="100,200,500,1000,2000,5000")
     ap.add_argument("--serve-duration", type=float, default=5.0, help="seconds of arrivals per rate")
     ap.add_argument("--serve-slice", type=int, default=262144, help="tiles per launch")
+    ap.add_argument("--serve-inflight", type=int, default=2, help="launches in flight (batched server)")
     ap.add_argument("--serve-timeout", type=float, default=300.0)
     ap.add_argument("--no-extras", dest="extras", action="store_false",
                     help="skip the sphere, noise and serving figures of the default run")
