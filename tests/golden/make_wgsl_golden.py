@@ -30,9 +30,13 @@ OUT = HERE / "wgsl_raycast.npz"
 # Grids: 0 the r=64 sphere, 1 the 2000-sphere grid, 2 40 small spheres spread over
 # [-6000, 6000)^3 (several N5 nodes, negative coordinates), 3 the noise grid's leaves
 # with origins in [0, 1024)^3, 4 spheres cut by the planes of the 345 grid tints
-# (coordinates that are multiples of 4096, 2048, 128 and 8).
+# (coordinates that are multiples of 4096, 2048, 128 and 8), 5 and 6 the reference's
+# own cube and icosahedron models (their topology as the reader took it from the
+# reference's assets, frozen in tests/golden/*_topology.npz), with the cameras of
+# tests/golden/*_render.npz.
 RANDOM_SPHERES = dict(count=40, rmin=3.0, rmax=12.0, lo=-6000.0, hi=6000.0, seed=11)
 NOISE_BOX = (0, 1024)
+MODELS = {5: "cube", 6: "icosahedron"}
 PLANE_SPHERES = np.array([[4096.0, 100.0, 100.0, 16.0], [2048.0, -50.0, 300.0, 16.0],
                           [-4096.0, 10.0, -4096.0, 20.0], [640.0, 384.0, 60.0, 10.0]])
 
@@ -52,6 +56,9 @@ def grid_view(g: int) -> dict:
         return O.workload_view("noise", box=NOISE_BOX)
     if g == 4:
         return O.Tree.spheres(PLANE_SPHERES, 3.0).view()
+    if g in MODELS:
+        t = np.load(HERE / f"{MODELS[g]}_topology.npz")
+        return O.Tree.from_masks({k: t[k] for k in ("kids5", "vals5", "kids4", "vals4", "vals3", "origins")}).view()
     raise ValueError(g)
 
 
@@ -118,6 +125,19 @@ def frames():
         eye = c[:3] + np.array([45.0, 25.0, 60.0])
         for mode, show in ((0, (1, 1, 1)), (1, (0, 1, 0)), (2, (1, 0, 1))):
             out.append((4, 64, 48, _state(eye, c[:3], 64, 48, mode, show), False))
+    # the reference's models: each frozen camera, and the first one in every mode
+    for g, name in MODELS.items():
+        r = np.load(HERE / f"{name}_render.npz")
+        k = 0
+        while f"state{k}" in r:
+            w, h = (int(x) for x in r[f"size{k}"])
+            st = r[f"state{k}"].tobytes()
+            modes = range(5) if k == 0 else (struct.unpack_from("<I", st, 192)[0],)
+            for mode in modes:
+                b = bytearray(st)
+                struct.pack_into("<I", b, 192, mode)
+                out.append((g, w, h, bytes(b), False))
+            k += 1
     return out
 
 

@@ -2,9 +2,10 @@
 
 tests/golden/wgsl_raycast.npz holds RGBA8 frames of src/shaders/raycast.comp.wgsl
 (woxel), translated mechanically to C++ by oracle/wgsl_ref.py and run on the host
-(tests/golden/make_wgsl_golden.py made them): 66 frames over five grids the oracle
+(tests/golden/make_wgsl_golden.py made them): 80 frames over seven grids the oracle
 builds (the r=64 sphere, the 2000-sphere grid, small spheres over several N5 nodes,
-noise leaves, spheres on the planes of the 345 grid tints), render modes 0-4, grid
+noise leaves, spheres on the planes of the 345 grid tints, and the reference's own
+cube and icosahedron models as its reader's topology), render modes 0-4, grid
 tints, cameras outside and inside the grids, rays with zero direction components and
 a -0 eye coordinate. Every frame must be equal byte for byte: the oracle's control
 flow, constants, index arithmetic and FP32 operation order are those of the shader
@@ -49,11 +50,11 @@ def test_fixture_recipes(golden):
     assert np.array_equal(golden["random_spheres"], mk.random_spheres())
     assert np.array_equal(golden["plane_spheres"], mk.PLANE_SPHERES)
     meta = golden["meta"]
-    assert len(meta) == 66 and set(int(g) for g in meta[:, 0]) == {0, 1, 2, 3, 4}
+    assert len(meta) == 80 and set(int(g) for g in meta[:, 0]) == {0, 1, 2, 3, 4, 5, 6}
     assert sum(int(x) for x in meta[:, 3]) == 1  # the 1920x1080 frame, checked on the GPU
 
 
-@pytest.mark.parametrize("grid", [0, 2, 3, 4])
+@pytest.mark.parametrize("grid", [0, 2, 3, 4, 5, 6])
 def test_oracle_matches_reference_shader(golden, grid):
     mk = _make()
     view = mk.grid_view(grid)

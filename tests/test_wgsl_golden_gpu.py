@@ -26,7 +26,7 @@ def golden():
 @pytest.fixture(scope="module")
 def grids(cuda_ctx, oracle_spheres_view):
     mk = _make()
-    views = {g: (oracle_spheres_view if g == 1 else mk.grid_view(g)) for g in range(5)}
+    views = {g: (oracle_spheres_view if g == 1 else mk.grid_view(g)) for g in range(7)}
     return {g: cuda_ctx.upload_view(v) for g, v in views.items()}
 
 
@@ -57,7 +57,7 @@ def test_kernels_with_hit_records_match_reference_shader(golden, cuda_ctx, grids
 
 
 def test_batched_launch_matches_reference_shader(golden, cuda_ctx, grids):
-    """All 66 frames over the five grids in one batched launch (the persistent kernel over
+    """All 80 frames over the seven grids in one batched launch (the persistent kernel over
     a job table, the path of wx_batch_* plans and the server), and again as a CUDA-graph
     plan replayed twice."""
     import torch
