@@ -29,7 +29,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true",
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread"]
 
 CU_SOURCES = ["kernels.cu", "sdf.cu"]
-CXX_SOURCES = ["api.cpp", "server.cpp", "topology.cpp", "scene.cpp", "vdbio.cpp"]
+CXX_SOURCES = ["api.cpp", "server.cpp", "topology.cpp", "scene.cpp", "vdbio.cpp", "inflate.cpp"]
 CUDA_INC = ["-I", "/usr/local/cuda/include"]
 
 

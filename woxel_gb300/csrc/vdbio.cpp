@@ -8,8 +8,9 @@
 // reference sets LeafData::Value exactly where the topology's leaf mask is set
 // (read.rs:610-620). wx_vdb_read_topology therefore does not parse the
 // tree-data section; wx_vdb_read_leaf_values does (read_tree_data, :571-629),
-// for the zero-crossing mode's level-set values. Blosc- or zip-compressed data
-// is rejected (WX_ERR_UNSUPPORTED).
+// for the zero-crossing mode's level-set values. Zip (zlib) compressed buffers
+// are decoded (inflate.cpp), as the reference does with flate2; blosc-compressed
+// grids are rejected (WX_ERR_UNSUPPORTED: no blosc codec in this build).
 
 #include <algorithm>
 #include <cstdio>
@@ -18,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "inflate.h"
 #include "wx_common.h"
 
 namespace {
@@ -121,6 +123,31 @@ struct Grid {
     Meta meta;
 };
 
+// read_compressed_data (read.rs:490-569): count values of elem bytes. Zip: an
+// int64 byte count n, then n bytes of a zlib stream that holds the count values,
+// or (n <= 0) -n / elem values stored as they are; otherwise the raw values. Blosc
+// is checked first, as in the reference. dst == nullptr skips the values.
+bool read_values(Reader &r, const Grid &g, size_t count, size_t elem, void *dst) {
+    if (g.compression & kBlosc) return r.fail("blosc-compressed grids are not supported");
+    if (!(g.compression & kZip)) return dst ? r.bytes(dst, count * elem) : r.skip((long)(count * elem));
+    const int64_t n = r.get<int64_t>();
+    if (!r.ok) return false;
+    if (n <= 0) {
+        const uint64_t k = (uint64_t)(-n) / elem;  // the reference reads this many values
+        if (k != count) return r.fail("zip block: stored value count differs from the node's");
+        return dst ? r.bytes(dst, count * elem) : r.skip((long)(count * elem));
+    }
+    if (!dst) return r.skip((long)n);
+    if (n > (int64_t)(64u << 20)) return r.fail("zip block larger than any node's values");
+    std::vector<uint8_t> z((size_t)n);
+    if (!r.bytes(z.data(), z.size())) return false;
+    std::string err;
+    const long long got = wx::zlib_inflate(z.data(), z.size(), static_cast<uint8_t *>(dst), count * elem, &err);
+    if (got < 0) return r.fail(err);
+    if ((size_t)got != count * elem) return r.fail("zip block holds fewer values than the node");
+    return true;
+}
+
 // read_compressed (read.rs:378-488) for a node header whose values are not
 // kept: consumes exactly the bytes the reference reads.
 bool skip_compressed(Reader &r, uint32_t version, const Grid &g, size_t size, const std::vector<uint64_t> &vmask) {
@@ -135,9 +162,7 @@ bool skip_compressed(Reader &r, uint32_t version, const Grid &g, size_t size, co
         count = 0;
         for (uint64_t w : vmask) count += (size_t)__builtin_popcountll(w);
     }
-    if (g.compression & (kBlosc | kZip)) return r.fail("blosc/zip-compressed grids are not supported");
-    r.skip((long)(count * (g.meta.half ? 2 : 4)));
-    return r.ok;
+    return read_values(r, g, count, g.meta.half ? 2 : 4, nullptr);
 }
 
 // Leaf buffers of the tree-data section (read_tree_data, read.rs:571-629, with
@@ -167,14 +192,13 @@ bool read_leaf_values(Reader &r, uint32_t version, const Grid &g, float backgrou
         count = 0;
         for (uint64_t w : vmask) count += (size_t)__builtin_popcountll(w);
     }
-    if (g.compression & (kBlosc | kZip)) return r.fail("blosc/zip-compressed grids are not supported");
     float data[512];
     if (g.meta.half) {
         uint16_t h[512];
-        r.bytes(h, count * 2);
-        for (size_t i = 0; i < count; i++) data[i] = half_to_float(h[i]);
+        read_values(r, g, count, 2, h);
+        for (size_t i = 0; i < count && r.ok; i++) data[i] = half_to_float(h[i]);
     } else {
-        r.bytes(data, count * 4);
+        read_values(r, g, count, 4, data);
     }
     if (!r.ok) return false;
     if (count == 512) {
