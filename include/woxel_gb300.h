@@ -404,9 +404,10 @@ int wx_topology_atlas(const wx_topology *topo, uint32_t side[3], uint32_t *a5, u
 
 /* ---- OpenVDB files: VdbReader::new + read_vdb345_grid (src/vdb/read.rs:62-349) ----
  * Reads the tree topology of one grid (grid_name NULL = the first) of an
- * uncompressed or active-mask-compressed file (the reference's assets use
- * flag 2: active mask, half-float values). Leaf values are not read: the march
- * only uses the value masks. Blosc/zip files give WX_ERR_UNSUPPORTED. */
+ * uncompressed, active-mask-compressed or zip (zlib) compressed file (the
+ * reference's assets use flag 2: active mask, half-float values; zip buffers are
+ * decoded as read.rs:546-563 decodes them). Leaf values are not read: the march
+ * only uses the value masks. Blosc-compressed grids give WX_ERR_UNSUPPORTED. */
 typedef struct wx_vdb_info {
     uint32_t file_version, compression, half_float, reserved;
     int64_t file_voxel_count; /* grid metadata "file_voxel_count", -1 if absent */
