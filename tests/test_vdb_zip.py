@@ -73,6 +73,17 @@ def test_zip_with_all_values_stored(tmp_path, leaves):
     assert_same(read(tmp_path / "raw.vdb"), read(tmp_path / "zip.vdb"))
 
 
+def test_zip_half_float(tmp_path, leaves):
+    """Half-float values (2-byte elements in the zip blocks), converted exactly."""
+    write(tmp_path / "raw.vdb", leaves, half=True)
+    write(tmp_path / "zip.vdb", leaves, compression=ACTIVE_MASK | ZIP, block=Block("zlib", 9), half=True)
+    a, b = read(tmp_path / "raw.vdb"), read(tmp_path / "zip.vdb")
+    assert a[1]["half_float"] and b[1]["half_float"]
+    assert_same(a, b)
+    written = sorted(np.where(m, v.astype(np.float16).astype(np.float32), 3.0).tobytes() for m, v in leaves.values())
+    assert sorted(a[2].reshape(-1, 512)[i].tobytes() for i in range(len(leaves))) == written
+
+
 def test_blosc_is_unsupported(tmp_path, leaves):
     write(tmp_path / "blosc.vdb", leaves, compression=ACTIVE_MASK | BLOSC, block=Block("zlib", 6))
     with pytest.raises(wx.WxError, match="blosc"):

@@ -49,9 +49,11 @@ class Block:
 
 
 def write(path, leaves: dict, background: float = 3.0, compression: int = ACTIVE_MASK,
-          block: Block = Block(), all_values: bool = False, voxel_count: int = -1) -> None:
+          block: Block = Block(), all_values: bool = False, voxel_count: int = -1, half: bool = False) -> None:
     """leaves: {(x, y, z) leaf origin (multiples of 8): (value mask bool[512], values float32[512])},
-    voxel offset (x & 7) << 6 | (y & 7) << 3 | (z & 7)."""
+    voxel offset (x & 7) << 6 | (y & 7) << 3 | (z & 7). half: values stored as IEEE binary16
+    (grid metadata is_saved_as_half_float)."""
+    vt = np.float16 if half else np.float32
     n5 = {}
     for o in leaves:
         k5 = tuple(c & ~4095 for c in o)
@@ -66,9 +68,9 @@ def write(path, leaves: dict, background: float = 3.0, compression: int = ACTIVE
 
     def node_values(nslots: int, vmask_words: np.ndarray) -> bytes:
         if all_values:  # metadata 6: every slot's value (the background here)
-            return bytes([6]) + block.encode(np.full(nslots, background, np.float32).tobytes())
+            return bytes([6]) + block.encode(np.full(nslots, background, vt).tobytes())
         n = int(sum(bin(int(w)).count("1") for w in vmask_words)) if compression & ACTIVE_MASK else nslots
-        return bytes([0]) + block.encode(np.full(n, background, np.float32).tobytes())
+        return bytes([0]) + block.encode(np.full(n, background, vt).tobytes())
 
     topo = bytearray()
     topo += struct.pack("<I", 1) + struct.pack("<f", background) + struct.pack("<II", 0, len(n5))
@@ -94,13 +96,16 @@ def write(path, leaves: dict, background: float = 3.0, compression: int = ACTIVE
         m, v = leaves[o]
         mw = _bits(np.flatnonzero(m), 512)
         data += mw.tobytes()
-        vals = np.asarray(v, np.float32)
+        vals = np.asarray(v, np.float32).astype(vt)
         if all_values or not (compression & ACTIVE_MASK):
             data += bytes([6]) + block.encode(vals.tobytes())
         else:
             data += bytes([0]) + block.encode(vals[np.asarray(m, bool)].tobytes())
 
-    meta = struct.pack("<I", 1) + _lstr("file_voxel_count") + _lstr("int64") + struct.pack("<Iq", 8, voxel_count)
+    meta = struct.pack("<I", 2 if half else 1) + _lstr("file_voxel_count") + _lstr("int64") + \
+        struct.pack("<Iq", 8, voxel_count)
+    if half:
+        meta += _lstr("is_saved_as_half_float") + _lstr("bool") + struct.pack("<IB", 1, 1)
     transform = _lstr("UniformScaleMap") + struct.pack("<15d", *([0.0] * 3 + [1.0] * 3 + [1.0] * 3 + [1.0] * 3 + [0.0] * 3))
     head = struct.pack("<QIIIB", 0x56444220, 224, 10, 0, 1) + b"0" * 36 + struct.pack("<I", 0) + struct.pack("<I", 1)
     desc = _lstr("ls") + _lstr("Tree_float_5_4_3") + _lstr("")
