@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -390,6 +391,21 @@ int parse(const char *path, const char *grid_name, wx_topology **out, wx_vdb_inf
     return WX_OK;
 }
 
+// parse() behind the C ABI: no exception crosses it (a host allocation that fails
+// while reading is WX_ERR_OOM).
+int parse_guarded(const char *path, const char *grid_name, wx_topology **out, wx_vdb_info *info,
+                  std::vector<float> *values, float *bg_out, const char *who) {
+    try {
+        return parse(path, grid_name, out, info, values, bg_out, who);
+    } catch (const std::bad_alloc &) {
+        wx::set_thread_error(std::string(who) + ": host allocation failed");
+        return WX_ERR_OOM;
+    } catch (...) {
+        wx::set_thread_error(std::string(who) + ": unexpected error while reading");
+        return WX_ERR_INVALID;
+    }
+}
+
 }  // namespace
 
 extern "C" int wx_vdb_read_topology(const char *path, const char *grid_name, wx_topology **out, wx_vdb_info *info) {
@@ -397,7 +413,7 @@ extern "C" int wx_vdb_read_topology(const char *path, const char *grid_name, wx_
         wx::set_thread_error("wx_vdb_read_topology: null argument");
         return WX_ERR_INVALID;
     }
-    return parse(path, grid_name, out, info, nullptr, nullptr, "wx_vdb_read_topology");
+    return parse_guarded(path, grid_name, out, info, nullptr, nullptr, "wx_vdb_read_topology");
 }
 
 extern "C" int wx_vdb_read_leaf_values(const char *path, const char *grid_name, float *values, uint64_t capacity,
@@ -407,7 +423,7 @@ extern "C" int wx_vdb_read_leaf_values(const char *path, const char *grid_name, 
         return WX_ERR_INVALID;
     }
     std::vector<float> v;
-    const int rc = parse(path, grid_name, nullptr, nullptr, &v, background, "wx_vdb_read_leaf_values");
+    const int rc = parse_guarded(path, grid_name, nullptr, nullptr, &v, background, "wx_vdb_read_leaf_values");
     if (rc != WX_OK) return rc;
     *count = v.size();
     if (values) {
