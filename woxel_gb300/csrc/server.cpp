@@ -142,7 +142,7 @@ struct wx_server {
     uint32_t *cancel_dev = nullptr, *cancel_host = nullptr;  // the cancel table and its page-locked source
     cudaStream_t ctl = nullptr;                             // carries cancel writes while launches run
     std::thread th;
-    bool stop = false, arena_ready = false;
+    bool stop = false, arena_ready = false, broken = false;
     uint64_t next_ticket = 1;
     wx_server_stats st{};
 
@@ -265,6 +265,23 @@ struct wx_server {
     void loop() {
         cudaSetDevice(device);
         std::unique_lock<std::mutex> lk(mu);
+        try {
+            schedule(lk);
+        } catch (...) {
+            // A host allocation failed inside the scheduler: stop scheduling, let the
+            // launches in flight finish (their outputs stay valid until destroy), and
+            // refuse new submissions (WX_ERR_OOM).
+            broken = true;
+            for (Slot &sl : slots)
+                if (sl.busy) {
+                    cudaEventSynchronize(sl.ev);
+                    sl.busy = false;
+                }
+            cv_done.notify_all();
+        }
+    }
+
+    void schedule(std::unique_lock<std::mutex> &lk) {
         for (;;) {
             retire();
             admit();
@@ -286,6 +303,18 @@ int sfail(int code, const std::string &msg) {
     wx::set_thread_error(msg);
     return code;
 }
+// Runs an entry point's body so that no exception crosses the C ABI: a failed host
+// allocation is WX_ERR_OOM.
+template <class F>
+int guarded(const char *who, F &&f) {
+    try {
+        return f();
+    } catch (const std::bad_alloc &) {
+        return sfail(WX_ERR_OOM, std::string(who) + ": host allocation failed");
+    } catch (...) {
+        return sfail(WX_ERR_INVALID, std::string(who) + ": unexpected error");
+    }
+}
 void fill_result(const Req *q, wx_result *o) {
     o->ticket = q->ticket;
     o->user = q->r.user;
@@ -303,289 +332,336 @@ void fill_result(const Req *q, wx_result *o) {
 extern "C" {
 
 int wx_server_create(wx_ctx *ctx, const wx_server_config *cfg, wx_server **out) {
-    if (!ctx || !cfg || !out) return sfail(WX_ERR_INVALID, "wx_server_create: null argument");
-    wx_server_config c = *cfg;
-    if (c.max_inflight == 0) c.max_inflight = 2;
-    // Default slice: four 1080p frames. Measured at saturation (5000 req/s over the 8
-    // benchmark grids): 3.58 Grays/s at 16,384 tiles per launch, 5.62 at 65,536, 5.90 at
-    // 262,144 and 5.94 at 1,048,576, with p50/p99 at 200-2000 req/s unchanged or better.
-    if (c.slice_tiles == 0) c.slice_tiles = 262144;
-    if (c.max_frames == 0) c.max_frames = 256;
-    if (c.max_inflight > 8 || c.max_frames > 1024)
-        return sfail(WX_ERR_INVALID, "wx_server_create: max_inflight must be <= 8 and max_frames <= 1024");
-    auto *s = new (std::nothrow) wx_server();
-    if (!s) return sfail(WX_ERR_OOM, "host allocation failed");
-    s->ctx = ctx;
-    s->cfg = c;
-    wxk::ctx_device_info(ctx, &s->device, &s->num_sms);
-    cudaSetDevice(s->device);
-    cudaError_t e;
-    auto bail = [&](cudaError_t err, const char *what) {
-        s->stop = true;
-        wx_server_destroy(s);
-        return sfail(err == cudaErrorMemoryAllocation ? WX_ERR_OOM : WX_ERR_CUDA,
-                     std::string(what) + ": " + cudaGetErrorString(err));
-    };
-    s->slots.resize(c.max_inflight);
-    for (Slot &sl : s->slots) {
-        if ((e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
-        if ((e = cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "event");
-        if ((e = wx::pinned_alloc(&sl.jobs_host, c.max_frames * sizeof(wxk::Job))) != cudaSuccess) return bail(e, "jobs");
-        if ((e = wx::dev_alloc(&sl.jobs_dev, c.max_frames * sizeof(wxk::Job))) != cudaSuccess) return bail(e, "jobs");
-        if ((e = wx::dev_alloc(&sl.counter, 256)) != cudaSuccess) return bail(e, "counter");
-        if ((e = wx::pinned_alloc(&sl.skipped_host, sizeof(uint32_t))) != cudaSuccess) return bail(e, "counter");
-        *sl.skipped_host = 0;
-    }
-    if ((e = wx::dev_alloc(&s->cancel_dev, kCancelSlots * sizeof(uint32_t))) != cudaSuccess) return bail(e, "cancel");
-    if ((e = wx::pinned_alloc(&s->cancel_host, kCancelSlots * sizeof(uint32_t))) != cudaSuccess)
-        return bail(e, "cancel");
-    if ((e = cudaMemset(s->cancel_dev, 0, kCancelSlots * sizeof(uint32_t))) != cudaSuccess) return bail(e, "cancel");
-    if ((e = cudaStreamCreateWithFlags(&s->ctl, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
-    s->th = std::thread([s] { s->loop(); });
-    *out = s;
-    return WX_OK;
+    return guarded("wx_server_create", [&]() -> int {
+        if (!ctx || !cfg || !out) return sfail(WX_ERR_INVALID, "wx_server_create: null argument");
+        wx_server_config c = *cfg;
+        if (c.max_inflight == 0) c.max_inflight = 2;
+        // Default slice: four 1080p frames. Measured at saturation (5000 req/s over the 8
+        // benchmark grids): 3.58 Grays/s at 16,384 tiles per launch, 5.62 at 65,536, 5.90 at
+        // 262,144 and 5.94 at 1,048,576, with p50/p99 at 200-2000 req/s unchanged or better.
+        if (c.slice_tiles == 0) c.slice_tiles = 262144;
+        if (c.max_frames == 0) c.max_frames = 256;
+        if (c.max_inflight > 8 || c.max_frames > 1024)
+            return sfail(WX_ERR_INVALID, "wx_server_create: max_inflight must be <= 8 and max_frames <= 1024");
+        auto *s = new (std::nothrow) wx_server();
+        if (!s) return sfail(WX_ERR_OOM, "host allocation failed");
+        s->ctx = ctx;
+        s->cfg = c;
+        wxk::ctx_device_info(ctx, &s->device, &s->num_sms);
+        cudaSetDevice(s->device);
+        cudaError_t e;
+        auto bail = [&](cudaError_t err, const char *what) {
+            s->stop = true;
+            wx_server_destroy(s);
+            return sfail(err == cudaErrorMemoryAllocation ? WX_ERR_OOM : WX_ERR_CUDA,
+                         std::string(what) + ": " + cudaGetErrorString(err));
+        };
+        try {  // host containers first; the scheduler then never grows a slot's parts list
+            s->slots.resize(c.max_inflight);
+            for (Slot &sl : s->slots) sl.parts.reserve(c.max_frames);
+        } catch (...) {
+            delete s;
+            throw;
+        }
+        for (Slot &sl : s->slots) {
+            if ((e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
+            if ((e = cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "event");
+            if ((e = wx::pinned_alloc(&sl.jobs_host, c.max_frames * sizeof(wxk::Job))) != cudaSuccess) return bail(e, "jobs");
+            if ((e = wx::dev_alloc(&sl.jobs_dev, c.max_frames * sizeof(wxk::Job))) != cudaSuccess) return bail(e, "jobs");
+            if ((e = wx::dev_alloc(&sl.counter, 256)) != cudaSuccess) return bail(e, "counter");
+            if ((e = wx::pinned_alloc(&sl.skipped_host, sizeof(uint32_t))) != cudaSuccess) return bail(e, "counter");
+            *sl.skipped_host = 0;
+        }
+        if ((e = wx::dev_alloc(&s->cancel_dev, kCancelSlots * sizeof(uint32_t))) != cudaSuccess) return bail(e, "cancel");
+        if ((e = wx::pinned_alloc(&s->cancel_host, kCancelSlots * sizeof(uint32_t))) != cudaSuccess)
+            return bail(e, "cancel");
+        if ((e = cudaMemset(s->cancel_dev, 0, kCancelSlots * sizeof(uint32_t))) != cudaSuccess) return bail(e, "cancel");
+        if ((e = cudaStreamCreateWithFlags(&s->ctl, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
+        try {
+            s->th = std::thread([s] { s->loop(); });
+        } catch (...) {
+            s->stop = true;
+            wx_server_destroy(s);
+            throw;
+        }
+        *out = s;
+        return WX_OK;
+    });
 }
 
 int wx_server_add_grid(wx_server *s, const wx_grid *grid, uint32_t *grid_id) {
-    if (!s || !grid || !grid_id) return sfail(WX_ERR_INVALID, "wx_server_add_grid: null argument");
-    wxk::DevGrid g;
-    int dev = -1;
-    wxk::grid_device_view(grid, &g, &dev);
-    if (dev != s->device) return sfail(WX_ERR_INVALID, "wx_server_add_grid: grid is on another device");
-    wx_grid_info info;
-    wx_grid_get_info(grid, &info);
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (s->arena_ready) return sfail(WX_ERR_INVALID, "wx_server_add_grid: add grids before the first request");
-    if (s->grid_bytes + info.device_bytes > s->cfg.budget_bytes)
-        return sfail(WX_ERR_BUDGET, "wx_server_add_grid: resident grids exceed the budget");
-    s->grids.push_back(g);
-    s->grid_bytes += info.device_bytes;
-    *grid_id = (uint32_t)s->grids.size() - 1;
-    return WX_OK;
+    return guarded("wx_server_add_grid", [&]() -> int {
+        if (!s || !grid || !grid_id) return sfail(WX_ERR_INVALID, "wx_server_add_grid: null argument");
+        wxk::DevGrid g;
+        int dev = -1;
+        wxk::grid_device_view(grid, &g, &dev);
+        if (dev != s->device) return sfail(WX_ERR_INVALID, "wx_server_add_grid: grid is on another device");
+        wx_grid_info info;
+        wx_grid_get_info(grid, &info);
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->arena_ready) return sfail(WX_ERR_INVALID, "wx_server_add_grid: add grids before the first request");
+        if (s->grid_bytes + info.device_bytes > s->cfg.budget_bytes)
+            return sfail(WX_ERR_BUDGET, "wx_server_add_grid: resident grids exceed the budget");
+        s->grids.push_back(g);
+        s->grid_bytes += info.device_bytes;
+        *grid_id = (uint32_t)s->grids.size() - 1;
+        return WX_OK;
+    });
 }
 
 int wx_server_submit(wx_server *s, const wx_request *r, uint64_t *ticket) {
-    if (!s || !r) return sfail(WX_ERR_INVALID, "wx_server_submit: null argument");
-    if ((uint64_t)r->width * r->height >= (1ull << 32)) return sfail(WX_ERR_UNSUPPORTED, "wx_server_submit: too large");
-    auto *q = new (std::nothrow) Req();
-    if (!q) return sfail(WX_ERR_OOM, "host allocation failed");
-    q->r = *r;
-    q->tiles = ((r->width & ~7u) / kTileW) * ((r->height & ~3u) / kTileH);
-    q->bytes = q->tiles ? (((size_t)r->width * r->height * 4 + 255) & ~(size_t)255) +
-                              (r->want_hits ? (size_t)r->width * r->height * sizeof(wx_hit) : 0)
-                        : 0;
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (r->grid_id >= s->grids.size()) {
-        delete q;
-        return sfail(WX_ERR_INVALID, "wx_server_submit: unknown grid_id");
-    }
-    if (!s->arena_ready) {
-        // The output arena takes the budget left after the resident grids,
-        // keeping 1 GiB of the device's free memory untouched.
-        cudaSetDevice(s->device);
-        size_t free_b = 0, total_b = 0;
-        cudaMemGetInfo(&free_b, &total_b);
-        const size_t margin = (size_t)1 << 30;
-        size_t bytes = s->cfg.budget_bytes - s->grid_bytes;
-        if (free_b > margin && bytes > free_b - margin) bytes = free_b - margin;
-        const cudaError_t e = s->arena.init(bytes);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
+    return guarded("wx_server_submit", [&]() -> int {
+        if (!s || !r) return sfail(WX_ERR_INVALID, "wx_server_submit: null argument");
+        if ((uint64_t)r->width * r->height >= (1ull << 32)) return sfail(WX_ERR_UNSUPPORTED, "wx_server_submit: too large");
+        auto *q = new (std::nothrow) Req();
+        if (!q) return sfail(WX_ERR_OOM, "host allocation failed");
+        q->r = *r;
+        q->tiles = ((r->width & ~7u) / kTileW) * ((r->height & ~3u) / kTileH);
+        q->bytes = q->tiles ? (((size_t)r->width * r->height * 4 + 255) & ~(size_t)255) +
+                                  (r->want_hits ? (size_t)r->width * r->height * sizeof(wx_hit) : 0)
+                            : 0;
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->broken) {
             delete q;
-            return sfail(WX_ERR_OOM, std::string("wx_server_submit: output arena: ") + cudaGetErrorString(e));
+            return sfail(WX_ERR_OOM, "wx_server_submit: the server stopped after a host allocation failure");
         }
-        s->arena_ready = true;
-    }
-    if (q->bytes > s->arena.size()) {
-        delete q;
-        return sfail(WX_ERR_BUDGET, "wx_server_submit: request larger than the output arena");
-    }
-    q->g = s->grids[r->grid_id];
-    q->ticket = s->next_ticket++;
-    q->t_submit = now_s();
-    s->reqs[q->ticket] = q;
-    s->pending.push_back(q);
-    s->st.submitted++;
-    if (ticket) *ticket = q->ticket;
-    s->cv_work.notify_one();
-    return WX_OK;
+        if (r->grid_id >= s->grids.size()) {
+            delete q;
+            return sfail(WX_ERR_INVALID, "wx_server_submit: unknown grid_id");
+        }
+        if (!s->arena_ready) {
+            // The output arena takes the budget left after the resident grids,
+            // keeping 1 GiB of the device's free memory untouched.
+            cudaSetDevice(s->device);
+            size_t free_b = 0, total_b = 0;
+            cudaMemGetInfo(&free_b, &total_b);
+            const size_t margin = (size_t)1 << 30;
+            size_t bytes = s->cfg.budget_bytes - s->grid_bytes;
+            if (free_b > margin && bytes > free_b - margin) bytes = free_b - margin;
+            const cudaError_t e = s->arena.init(bytes);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                delete q;
+                return sfail(WX_ERR_OOM, std::string("wx_server_submit: output arena: ") + cudaGetErrorString(e));
+            }
+            s->arena_ready = true;
+        }
+        if (q->bytes > s->arena.size()) {
+            delete q;
+            return sfail(WX_ERR_BUDGET, "wx_server_submit: request larger than the output arena");
+        }
+        q->g = s->grids[r->grid_id];
+        q->ticket = s->next_ticket++;
+        q->t_submit = now_s();
+        try {  // a failed insertion leaves neither container holding q
+            s->reqs.emplace(q->ticket, q);
+        } catch (...) {
+            delete q;
+            throw;
+        }
+        try {
+            s->pending.push_back(q);
+        } catch (...) {
+            s->reqs.erase(q->ticket);
+            delete q;
+            throw;
+        }
+        s->st.submitted++;
+        if (ticket) *ticket = q->ticket;
+        s->cv_work.notify_one();
+        return WX_OK;
+    });
 }
 
 int wx_server_cancel(wx_server *s, uint64_t ticket) {
-    if (!s) return WX_ERR_INVALID;
-    std::lock_guard<std::mutex> lk(s->mu);
-    auto it = s->reqs.find(ticket);
-    if (it == s->reqs.end()) return sfail(WX_ERR_INVALID, "wx_server_cancel: unknown ticket");
-    Req *q = it->second;
-    if (q->state == RState::Pending) {
-        s->pending.erase(std::find(s->pending.begin(), s->pending.end(), q));
-        s->finish(q, WX_ERR_CANCELLED);
+    return guarded("wx_server_cancel", [&]() -> int {
+        if (!s) return WX_ERR_INVALID;
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->reqs.find(ticket);
+        if (it == s->reqs.end()) return sfail(WX_ERR_INVALID, "wx_server_cancel: unknown ticket");
+        Req *q = it->second;
+        if (q->state == RState::Pending) {
+            s->pending.erase(std::find(s->pending.begin(), s->pending.end(), q));
+            s->finish(q, WX_ERR_CANCELLED);
+            return WX_OK;
+        }
+        if (q->state != RState::Active) return sfail(WX_ERR_INVALID, "wx_server_cancel: request already finished");
+        if (q->status == WX_OK) {
+            // Tiles not yet launched are dropped by the scheduler; launches on the GPU
+            // skip the rest once the ticket lands in the cancel table (copied on the
+            // control stream, concurrently with them). The request finishes with
+            // WX_ERR_CANCELLED when no launch refers to it any more.
+            q->status = WX_ERR_CANCELLED;
+            const uint32_t slot = (uint32_t)(q->ticket % kCancelSlots);
+            s->cancel_host[slot] = (uint32_t)q->ticket;
+            int prev = -1;
+            cudaGetDevice(&prev);
+            if (prev != s->device) cudaSetDevice(s->device);
+            const cudaError_t e = cudaMemcpyAsync(s->cancel_dev + slot, s->cancel_host + slot, sizeof(uint32_t),
+                                                  cudaMemcpyHostToDevice, s->ctl);
+            if (prev != s->device && prev >= 0) cudaSetDevice(prev);
+            if (e != cudaSuccess) cudaGetLastError();  // the launched tiles then just render
+        }
+        s->cv_work.notify_one();
         return WX_OK;
-    }
-    if (q->state != RState::Active) return sfail(WX_ERR_INVALID, "wx_server_cancel: request already finished");
-    if (q->status == WX_OK) {
-        // Tiles not yet launched are dropped by the scheduler; launches on the GPU
-        // skip the rest once the ticket lands in the cancel table (copied on the
-        // control stream, concurrently with them). The request finishes with
-        // WX_ERR_CANCELLED when no launch refers to it any more.
-        q->status = WX_ERR_CANCELLED;
-        const uint32_t slot = (uint32_t)(q->ticket % kCancelSlots);
-        s->cancel_host[slot] = (uint32_t)q->ticket;
-        int prev = -1;
-        cudaGetDevice(&prev);
-        if (prev != s->device) cudaSetDevice(s->device);
-        const cudaError_t e = cudaMemcpyAsync(s->cancel_dev + slot, s->cancel_host + slot, sizeof(uint32_t),
-                                              cudaMemcpyHostToDevice, s->ctl);
-        if (prev != s->device && prev >= 0) cudaSetDevice(prev);
-        if (e != cudaSuccess) cudaGetLastError();  // the launched tiles then just render
-    }
-    s->cv_work.notify_one();
-    return WX_OK;
+    });
 }
 
 int wx_server_poll(wx_server *s, wx_result *out, uint32_t max, uint32_t *n, int wait_ms) {
-    if (!s || !n || (max && !out)) return sfail(WX_ERR_INVALID, "wx_server_poll: null argument");
-    std::unique_lock<std::mutex> lk(s->mu);
-    if (s->done_q.empty() && wait_ms > 0)
-        s->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] { return !s->done_q.empty(); });
-    uint32_t k = 0;
-    while (k < max && !s->done_q.empty()) {
-        Req *q = s->done_q.front();
-        s->done_q.pop_front();
-        q->state = RState::Polled;
-        fill_result(q, &out[k++]);
-    }
-    *n = k;
-    return WX_OK;
+    return guarded("wx_server_poll", [&]() -> int {
+        if (!s || !n || (max && !out)) return sfail(WX_ERR_INVALID, "wx_server_poll: null argument");
+        std::unique_lock<std::mutex> lk(s->mu);
+        if (s->done_q.empty() && wait_ms > 0)
+            s->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] { return !s->done_q.empty(); });
+        uint32_t k = 0;
+        while (k < max && !s->done_q.empty()) {
+            Req *q = s->done_q.front();
+            s->done_q.pop_front();
+            q->state = RState::Polled;
+            fill_result(q, &out[k++]);
+        }
+        *n = k;
+        return WX_OK;
+    });
 }
 
 int wx_server_copy_result(wx_server *s, uint64_t ticket, uint8_t *rgba8_host, wx_hit *hits_host) {
-    if (!s) return WX_ERR_INVALID;
-    const Req *q;
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        auto it = s->reqs.find(ticket);
-        if (it == s->reqs.end()) return sfail(WX_ERR_INVALID, "wx_server_copy_result: unknown ticket");
-        q = it->second;
-        if (q->state != RState::Polled) return sfail(WX_ERR_INVALID, "wx_server_copy_result: result not polled yet");
-        if (q->status != WX_OK) return sfail(WX_ERR_INVALID, "wx_server_copy_result: request did not complete");
-    }
-    // A polled request is only freed by wx_server_release on the caller's thread.
-    cudaSetDevice(s->device);
-    const size_t npix = (size_t)q->r.width * q->r.height;
-    if (rgba8_host && q->rgba && cudaMemcpy(rgba8_host, q->rgba, npix * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
-        return sfail(WX_ERR_CUDA, "wx_server_copy_result: copy failed");
-    if (hits_host && q->hits &&
-        cudaMemcpy(hits_host, q->hits, npix * sizeof(wx_hit), cudaMemcpyDeviceToHost) != cudaSuccess)
-        return sfail(WX_ERR_CUDA, "wx_server_copy_result: copy failed");
-    return WX_OK;
+    return guarded("wx_server_copy_result", [&]() -> int {
+        if (!s) return WX_ERR_INVALID;
+        const Req *q;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            auto it = s->reqs.find(ticket);
+            if (it == s->reqs.end()) return sfail(WX_ERR_INVALID, "wx_server_copy_result: unknown ticket");
+            q = it->second;
+            if (q->state != RState::Polled) return sfail(WX_ERR_INVALID, "wx_server_copy_result: result not polled yet");
+            if (q->status != WX_OK) return sfail(WX_ERR_INVALID, "wx_server_copy_result: request did not complete");
+        }
+        // A polled request is only freed by wx_server_release on the caller's thread.
+        cudaSetDevice(s->device);
+        const size_t npix = (size_t)q->r.width * q->r.height;
+        if (rgba8_host && q->rgba && cudaMemcpy(rgba8_host, q->rgba, npix * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return sfail(WX_ERR_CUDA, "wx_server_copy_result: copy failed");
+        if (hits_host && q->hits &&
+            cudaMemcpy(hits_host, q->hits, npix * sizeof(wx_hit), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return sfail(WX_ERR_CUDA, "wx_server_copy_result: copy failed");
+        return WX_OK;
+    });
 }
 
 int wx_server_release(wx_server *s, uint64_t ticket) {
-    if (!s) return WX_ERR_INVALID;
-    std::lock_guard<std::mutex> lk(s->mu);
-    auto it = s->reqs.find(ticket);
-    if (it == s->reqs.end()) return sfail(WX_ERR_INVALID, "wx_server_release: unknown ticket");
-    Req *q = it->second;
-    if (q->state != RState::Polled) return sfail(WX_ERR_INVALID, "wx_server_release: result not polled yet");
-    if (q->has_buf) s->arena.release(q->off, q->bytes);
-    s->reqs.erase(it);
-    delete q;
-    s->cv_work.notify_one();
-    return WX_OK;
+    return guarded("wx_server_release", [&]() -> int {
+        if (!s) return WX_ERR_INVALID;
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->reqs.find(ticket);
+        if (it == s->reqs.end()) return sfail(WX_ERR_INVALID, "wx_server_release: unknown ticket");
+        Req *q = it->second;
+        if (q->state != RState::Polled) return sfail(WX_ERR_INVALID, "wx_server_release: result not polled yet");
+        if (q->has_buf) s->arena.release(q->off, q->bytes);
+        s->reqs.erase(it);
+        delete q;
+        s->cv_work.notify_one();
+        return WX_OK;
+    });
 }
 
 int wx_server_get_stats(wx_server *s, wx_server_stats *o) {
-    if (!s || !o) return WX_ERR_INVALID;
-    std::lock_guard<std::mutex> lk(s->mu);
-    *o = s->st;
-    o->arena_bytes = s->arena.size();
-    o->arena_in_use = s->arena.in_use();
-    o->arena_peak = s->arena.peak();
-    o->pending = s->pending.size();
-    o->active = s->active.size();
-    return WX_OK;
+    return guarded("wx_server_get_stats", [&]() -> int {
+        if (!s || !o) return WX_ERR_INVALID;
+        std::lock_guard<std::mutex> lk(s->mu);
+        *o = s->st;
+        o->arena_bytes = s->arena.size();
+        o->arena_in_use = s->arena.in_use();
+        o->arena_peak = s->arena.peak();
+        o->pending = s->pending.size();
+        o->active = s->active.size();
+        return WX_OK;
+    });
 }
 
 int wx_server_replay(wx_server *s, const wx_request *reqs, const double *arrival_s, uint32_t n, wx_result *results,
                      int release, double timeout_s) {
-    if (!s || (n && (!reqs || !arrival_s || !results))) return sfail(WX_ERR_INVALID, "wx_server_replay: null argument");
-    std::unordered_map<uint64_t, uint32_t> index;
-    index.reserve(n * 2);
-    const double t0 = now_s();
-    uint32_t submitted = 0, collected = 0;
-    std::vector<wx_result> buf(64);
-    auto collect = [&](int wait_ms) {
-        uint32_t got = 0;
-        wx_server_poll(s, buf.data(), (uint32_t)buf.size(), &got, wait_ms);
-        for (uint32_t k = 0; k < got; k++) {
-            auto it = index.find(buf[k].ticket);
-            if (it == index.end()) continue;  // not ours
-            results[it->second] = buf[k];
-            collected++;
-            if (release) {
-                wx_server_release(s, buf[k].ticket);
-                results[it->second].rgba8 = nullptr;
-                results[it->second].hits = nullptr;
+    return guarded("wx_server_replay", [&]() -> int {
+        if (!s || (n && (!reqs || !arrival_s || !results))) return sfail(WX_ERR_INVALID, "wx_server_replay: null argument");
+        std::unordered_map<uint64_t, uint32_t> index;
+        index.reserve(n * 2);
+        const double t0 = now_s();
+        uint32_t submitted = 0, collected = 0;
+        std::vector<wx_result> buf(64);
+        auto collect = [&](int wait_ms) {
+            uint32_t got = 0;
+            wx_server_poll(s, buf.data(), (uint32_t)buf.size(), &got, wait_ms);
+            for (uint32_t k = 0; k < got; k++) {
+                auto it = index.find(buf[k].ticket);
+                if (it == index.end()) continue;  // not ours
+                results[it->second] = buf[k];
+                collected++;
+                if (release) {
+                    wx_server_release(s, buf[k].ticket);
+                    results[it->second].rgba8 = nullptr;
+                    results[it->second].hits = nullptr;
+                }
             }
-        }
-    };
-    while (submitted < n) {
-        const double due = t0 + arrival_s[submitted];
-        for (;;) {
-            const double left = due - now_s();
-            if (left <= 0) break;
-            if (left > 200e-6) {
-                collect(0);
-                std::this_thread::sleep_for(std::chrono::duration<double>(std::min(left - 100e-6, 1e-3)));
+        };
+        while (submitted < n) {
+            const double due = t0 + arrival_s[submitted];
+            for (;;) {
+                const double left = due - now_s();
+                if (left <= 0) break;
+                if (left > 200e-6) {
+                    collect(0);
+                    std::this_thread::sleep_for(std::chrono::duration<double>(std::min(left - 100e-6, 1e-3)));
+                }
             }
+            uint64_t ticket = 0;
+            const int rc = wx_server_submit(s, &reqs[submitted], &ticket);
+            if (rc != WX_OK) return rc;
+            index[ticket] = submitted++;
+            if (now_s() - t0 > timeout_s) return sfail(WX_ERR_TIMEOUT, "wx_server_replay: timed out while submitting");
         }
-        uint64_t ticket = 0;
-        const int rc = wx_server_submit(s, &reqs[submitted], &ticket);
-        if (rc != WX_OK) return rc;
-        index[ticket] = submitted++;
-        if (now_s() - t0 > timeout_s) return sfail(WX_ERR_TIMEOUT, "wx_server_replay: timed out while submitting");
-    }
-    while (collected < n) {
-        if (now_s() - t0 > timeout_s) return sfail(WX_ERR_TIMEOUT, "wx_server_replay: timed out waiting for results");
-        collect(5);
-    }
-    return WX_OK;
+        while (collected < n) {
+            if (now_s() - t0 > timeout_s) return sfail(WX_ERR_TIMEOUT, "wx_server_replay: timed out waiting for results");
+            collect(5);
+        }
+        return WX_OK;
+    });
 }
 
 int wx_server_destroy(wx_server *s) {
-    if (!s) return WX_OK;
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        s->stop = true;
-        // Unadmitted requests will never run.
-        while (!s->pending.empty()) {
-            s->finish(s->pending.front(), WX_ERR_CANCELLED);
-            s->pending.pop_front();
+    return guarded("wx_server_destroy", [&]() -> int {
+        if (!s) return WX_OK;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stop = true;
+            // Unadmitted requests will never run.
+            while (!s->pending.empty()) {
+                s->finish(s->pending.front(), WX_ERR_CANCELLED);
+                s->pending.pop_front();
+            }
+            s->cv_work.notify_all();
         }
-        s->cv_work.notify_all();
-    }
-    if (s->th.joinable()) s->th.join();
-    cudaSetDevice(s->device);
-    for (Slot &sl : s->slots) {
-        if (sl.stream) cudaStreamSynchronize(sl.stream);
-        if (sl.ev) cudaEventDestroy(sl.ev);
-        if (sl.stream) cudaStreamDestroy(sl.stream);
-        if (sl.jobs_host) cudaFreeHost(sl.jobs_host);
-        if (sl.jobs_dev) cudaFree(sl.jobs_dev);
-        if (sl.counter) cudaFree(sl.counter);
-        if (sl.skipped_host) cudaFreeHost(sl.skipped_host);
-    }
-    if (s->ctl) {
-        cudaStreamSynchronize(s->ctl);
-        cudaStreamDestroy(s->ctl);
-    }
-    if (s->cancel_dev) cudaFree(s->cancel_dev);
-    if (s->cancel_host) cudaFreeHost(s->cancel_host);
-    s->arena.destroy();
-    for (auto &kv : s->reqs) delete kv.second;
-    delete s;
-    return WX_OK;
+        if (s->th.joinable()) s->th.join();
+        cudaSetDevice(s->device);
+        for (Slot &sl : s->slots) {
+            if (sl.stream) cudaStreamSynchronize(sl.stream);
+            if (sl.ev) cudaEventDestroy(sl.ev);
+            if (sl.stream) cudaStreamDestroy(sl.stream);
+            if (sl.jobs_host) cudaFreeHost(sl.jobs_host);
+            if (sl.jobs_dev) cudaFree(sl.jobs_dev);
+            if (sl.counter) cudaFree(sl.counter);
+            if (sl.skipped_host) cudaFreeHost(sl.skipped_host);
+        }
+        if (s->ctl) {
+            cudaStreamSynchronize(s->ctl);
+            cudaStreamDestroy(s->ctl);
+        }
+        if (s->cancel_dev) cudaFree(s->cancel_dev);
+        if (s->cancel_host) cudaFreeHost(s->cancel_host);
+        s->arena.destroy();
+        for (auto &kv : s->reqs) delete kv.second;
+        delete s;
+        return WX_OK;
+    });
 }
 
 }  // extern "C"
