@@ -499,69 +499,71 @@ int wx_ctx_get_tuning(const wx_ctx *ctx, wx_tuning *t) {
 
 int wx_autotune(wx_ctx *ctx, const wx_frame *frames, uint32_t n, const wx_tuning *candidates, uint32_t ncand,
                 uint32_t reps, wx_tuning *best, double *times_ms) {
-    if (!ctx || !frames || n == 0 || !best) return fail(ctx, WX_ERR_INVALID, "wx_autotune: null argument");
-    WX_CUDA(ctx, cudaSetDevice(ctx->device));
-    std::vector<wx_tuning> cand;
-    if (candidates) {
-        cand.assign(candidates, candidates + ncand);
-    } else {
-        for (int order : {1, 0}) {
-            for (int kernel : {0, 1})
-                for (int tw : {4, 8, 16})
-                    for (int wpb : {2, 4, 8}) cand.push_back(wx_tuning{kernel, wpb, 0, tw, order, 1});
-            // Occupancy of the persistent kernel: fewer resident warps than fit (16 per SM).
-            for (int tw : {4, 8}) cand.push_back(wx_tuning{0, 4, 4, tw, order, 1});
-            // Rays per lane: warps of several tiles whose lanes refill.
-            for (int rays : {2, 4, 8})
-                for (int tw : {4, 8})
-                    for (int wpb : {2, 4}) cand.push_back(wx_tuning{1, wpb, 0, tw, order, rays});
+    return wx::guard("wx_autotune", [&]() -> int {
+        if (!ctx || !frames || n == 0 || !best) return fail(ctx, WX_ERR_INVALID, "wx_autotune: null argument");
+        WX_CUDA(ctx, cudaSetDevice(ctx->device));
+        std::vector<wx_tuning> cand;
+        if (candidates) {
+            cand.assign(candidates, candidates + ncand);
+        } else {
+            for (int order : {1, 0}) {
+                for (int kernel : {0, 1})
+                    for (int tw : {4, 8, 16})
+                        for (int wpb : {2, 4, 8}) cand.push_back(wx_tuning{kernel, wpb, 0, tw, order, 1});
+                // Occupancy of the persistent kernel: fewer resident warps than fit (16 per SM).
+                for (int tw : {4, 8}) cand.push_back(wx_tuning{0, 4, 4, tw, order, 1});
+                // Rays per lane: warps of several tiles whose lanes refill.
+                for (int rays : {2, 4, 8})
+                    for (int tw : {4, 8})
+                        for (int wpb : {2, 4}) cand.push_back(wx_tuning{1, wpb, 0, tw, order, rays});
+            }
+            if (cand.size() != WX_AUTOTUNE_BUILTIN) return fail(ctx, WX_ERR_INVALID, "wx_autotune: built-in set size");
         }
-        if (cand.size() != WX_AUTOTUNE_BUILTIN) return fail(ctx, WX_ERR_INVALID, "wx_autotune: built-in set size");
-    }
-    if (cand.empty()) return fail(ctx, WX_ERR_INVALID, "wx_autotune: no candidates");
-    for (uint32_t i = 0; i < n; i++)
-        if (!frames[i].grid || !frames[i].rgba8 || !device_accessible(frames[i].rgba8))
-            return fail(ctx, WX_ERR_INVALID, "wx_autotune: frames need a grid and device rgba8");
-    const wxk::Tuning saved = ctx->tuning;
-    cudaEvent_t e0, e1;
-    WX_CUDA(ctx, cudaEventCreate(&e0));
-    WX_CUDA(ctx, cudaEventCreate(&e1));
-    cudaStream_t st;
-    WX_CUDA(ctx, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    double best_ms = 1e300;
-    size_t best_i = 0;
-    int rc = WX_OK;
-    for (size_t c = 0; c < cand.size() && rc == WX_OK; c++) {
-        rc = wx_ctx_set_tuning(ctx, &cand[c]);
-        if (rc != WX_OK) break;
-        double total = 0;
-        for (uint32_t rep = 0; rep <= reps && rc == WX_OK; rep++) {  // pass 0 warms up
-            cudaEventRecord(e0, st);
-            for (uint32_t i = 0; i < n && rc == WX_OK; i++)
-                rc = wx_render(ctx, frames[i].grid, &frames[i].state, frames[i].width, frames[i].height,
-                               frames[i].rgba8, frames[i].hits, st);
-            cudaEventRecord(e1, st);
-            cudaEventSynchronize(e1);
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (rep > 0) total += ms;
+        if (cand.empty()) return fail(ctx, WX_ERR_INVALID, "wx_autotune: no candidates");
+        for (uint32_t i = 0; i < n; i++)
+            if (!frames[i].grid || !frames[i].rgba8 || !device_accessible(frames[i].rgba8))
+                return fail(ctx, WX_ERR_INVALID, "wx_autotune: frames need a grid and device rgba8");
+        const wxk::Tuning saved = ctx->tuning;
+        cudaEvent_t e0, e1;
+        WX_CUDA(ctx, cudaEventCreate(&e0));
+        WX_CUDA(ctx, cudaEventCreate(&e1));
+        cudaStream_t st;
+        WX_CUDA(ctx, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        double best_ms = 1e300;
+        size_t best_i = 0;
+        int rc = WX_OK;
+        for (size_t c = 0; c < cand.size() && rc == WX_OK; c++) {
+            rc = wx_ctx_set_tuning(ctx, &cand[c]);
+            if (rc != WX_OK) break;
+            double total = 0;
+            for (uint32_t rep = 0; rep <= reps && rc == WX_OK; rep++) {  // pass 0 warms up
+                cudaEventRecord(e0, st);
+                for (uint32_t i = 0; i < n && rc == WX_OK; i++)
+                    rc = wx_render(ctx, frames[i].grid, &frames[i].state, frames[i].width, frames[i].height,
+                                   frames[i].rgba8, frames[i].hits, st);
+                cudaEventRecord(e1, st);
+                cudaEventSynchronize(e1);
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (rep > 0) total += ms;
+            }
+            const double mean = total / (reps ? reps : 1);
+            if (times_ms) times_ms[c] = mean;
+            if (rc == WX_OK && mean < best_ms) {
+                best_ms = mean;
+                best_i = c;
+            }
         }
-        const double mean = total / (reps ? reps : 1);
-        if (times_ms) times_ms[c] = mean;
-        if (rc == WX_OK && mean < best_ms) {
-            best_ms = mean;
-            best_i = c;
+        cudaStreamDestroy(st);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (rc != WX_OK) {
+            ctx->tuning = saved;
+            return rc;
         }
-    }
-    cudaStreamDestroy(st);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (rc != WX_OK) {
-        ctx->tuning = saved;
-        return rc;
-    }
-    *best = cand[best_i];
-    return wx_ctx_set_tuning(ctx, best);
+        *best = cand[best_i];
+        return wx_ctx_set_tuning(ctx, best);
+    });
 }
 
 int wx_check_division(wx_ctx *ctx, uint32_t max_m, uint64_t out[3]) {
@@ -1025,82 +1027,86 @@ static int build_jobs(wx_ctx *ctx, const wx_frame *frames, uint32_t n, std::vect
 }
 
 int wx_render_batch(wx_ctx *ctx, const wx_frame *frames, uint32_t n, void *stream) {
-    if (!ctx || (n && !frames)) return fail(ctx, WX_ERR_INVALID, "wx_render_batch: null argument");
-    WX_CUDA(ctx, cudaSetDevice(ctx->device));
-    std::vector<wxk::Job> jobs;
-    uint32_t total = 0;
-    uint64_t rays = 0;
-    int rc = build_jobs(ctx, frames, n, jobs, &total, &rays);
-    if (rc != WX_OK) return rc;
-    if (jobs.empty()) return WX_OK;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // The pinned staging table is reused: wait for the previous batch's copy.
-    WX_CUDA(ctx, cudaEventSynchronize(ctx->jobs_done));
-    if (jobs.size() > ctx->jobs_cap) {
-        if (ctx->jobs_dev) {
-            WX_CUDA(ctx, cudaDeviceSynchronize());
-            cudaFree(ctx->jobs_dev);
-            cudaFreeHost(ctx->jobs_host);
+    return wx::guard("wx_render_batch", [&]() -> int {
+        if (!ctx || (n && !frames)) return fail(ctx, WX_ERR_INVALID, "wx_render_batch: null argument");
+        WX_CUDA(ctx, cudaSetDevice(ctx->device));
+        std::vector<wxk::Job> jobs;
+        uint32_t total = 0;
+        uint64_t rays = 0;
+        int rc = build_jobs(ctx, frames, n, jobs, &total, &rays);
+        if (rc != WX_OK) return rc;
+        if (jobs.empty()) return WX_OK;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        // The pinned staging table is reused: wait for the previous batch's copy.
+        WX_CUDA(ctx, cudaEventSynchronize(ctx->jobs_done));
+        if (jobs.size() > ctx->jobs_cap) {
+            if (ctx->jobs_dev) {
+                WX_CUDA(ctx, cudaDeviceSynchronize());
+                cudaFree(ctx->jobs_dev);
+                cudaFreeHost(ctx->jobs_host);
+            }
+            ctx->jobs_dev = nullptr;
+            ctx->jobs_host = nullptr;
+            ctx->jobs_cap = 0;
+            const size_t cap = std::max<size_t>(jobs.size(), 256);
+            WX_CUDA(ctx, wx::dev_alloc(&ctx->jobs_dev, cap * sizeof(wxk::Job)));
+            WX_CUDA(ctx, wx::pinned_alloc(&ctx->jobs_host, cap * sizeof(wxk::Job)));
+            ctx->jobs_cap = cap;
         }
-        ctx->jobs_dev = nullptr;
-        ctx->jobs_host = nullptr;
-        ctx->jobs_cap = 0;
-        const size_t cap = std::max<size_t>(jobs.size(), 256);
-        WX_CUDA(ctx, wx::dev_alloc(&ctx->jobs_dev, cap * sizeof(wxk::Job)));
-        WX_CUDA(ctx, wx::pinned_alloc(&ctx->jobs_host, cap * sizeof(wxk::Job)));
-        ctx->jobs_cap = cap;
-    }
-    memcpy(ctx->jobs_host, jobs.data(), jobs.size() * sizeof(wxk::Job));
-    WX_CUDA(ctx, cudaMemcpyAsync(ctx->jobs_dev, ctx->jobs_host, jobs.size() * sizeof(wxk::Job),
-                                 cudaMemcpyHostToDevice, st));
-    WX_CUDA(ctx, cudaEventRecord(ctx->jobs_done, st));
-    WX_CUDA(ctx, wxk::launch_batched(ctx->jobs_dev, (uint32_t)jobs.size(), total, ctx->take_counter(), ctx->tuning,
-                                     ctx->num_sms, wxk::all_modes(jobs.data(), jobs.size()), st));
-    return WX_OK;
+        memcpy(ctx->jobs_host, jobs.data(), jobs.size() * sizeof(wxk::Job));
+        WX_CUDA(ctx, cudaMemcpyAsync(ctx->jobs_dev, ctx->jobs_host, jobs.size() * sizeof(wxk::Job),
+                                     cudaMemcpyHostToDevice, st));
+        WX_CUDA(ctx, cudaEventRecord(ctx->jobs_done, st));
+        WX_CUDA(ctx, wxk::launch_batched(ctx->jobs_dev, (uint32_t)jobs.size(), total, ctx->take_counter(), ctx->tuning,
+                                         ctx->num_sms, wxk::all_modes(jobs.data(), jobs.size()), st));
+        return WX_OK;
+    });
 }
 
 int wx_batch_create(wx_ctx *ctx, const wx_frame *frames, uint32_t n, wx_batch **out) {
-    if (!ctx || !out || (n && !frames)) return fail(ctx, WX_ERR_INVALID, "wx_batch_create: null argument");
-    WX_CUDA(ctx, cudaSetDevice(ctx->device));
-    std::vector<wxk::Job> jobs;
-    uint32_t total = 0;
-    uint64_t rays = 0;
-    int rc = build_jobs(ctx, frames, n, jobs, &total, &rays);
-    if (rc != WX_OK) return rc;
-    auto *b = new (std::nothrow) wx_batch();
-    if (!b) return fail(ctx, WX_ERR_OOM, "host allocation failed");
-    b->ctx = ctx;
-    b->njobs = (uint32_t)jobs.size();
-    b->total_tiles = total;
-    b->rays = rays;
-    auto bail = [&](cudaError_t e, const char *what) {
-        wx_batch_destroy(b);
-        return cuda_fail(ctx, e, what);
-    };
-    cudaError_t e;
-    if ((e = wx::dev_alloc(&b->jobs_dev, std::max<size_t>(jobs.size(), 1) * sizeof(wxk::Job))) != cudaSuccess)
-        return bail(e, "cudaMalloc(job table)");
-    if (!jobs.empty() &&
-        (e = cudaMemcpy(b->jobs_dev, jobs.data(), jobs.size() * sizeof(wxk::Job), cudaMemcpyHostToDevice)) != cudaSuccess)
-        return bail(e, "cudaMemcpy(job table)");
-    if ((e = wx::dev_alloc(&b->counter, sizeof(uint32_t))) != cudaSuccess) return bail(e, "cudaMalloc(counter)");
-    // Capture counter reset + persistent launch into a graph, replayed by wx_batch_launch.
-    cudaStream_t cs;
-    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
-    if ((e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+    return wx::guard("wx_batch_create", [&]() -> int {
+        if (!ctx || !out || (n && !frames)) return fail(ctx, WX_ERR_INVALID, "wx_batch_create: null argument");
+        WX_CUDA(ctx, cudaSetDevice(ctx->device));
+        std::vector<wxk::Job> jobs;
+        uint32_t total = 0;
+        uint64_t rays = 0;
+        int rc = build_jobs(ctx, frames, n, jobs, &total, &rays);
+        if (rc != WX_OK) return rc;
+        auto *b = new (std::nothrow) wx_batch();
+        if (!b) return fail(ctx, WX_ERR_OOM, "host allocation failed");
+        b->ctx = ctx;
+        b->njobs = (uint32_t)jobs.size();
+        b->total_tiles = total;
+        b->rays = rays;
+        auto bail = [&](cudaError_t e, const char *what) {
+            wx_batch_destroy(b);
+            return cuda_fail(ctx, e, what);
+        };
+        cudaError_t e;
+        if ((e = wx::dev_alloc(&b->jobs_dev, std::max<size_t>(jobs.size(), 1) * sizeof(wxk::Job))) != cudaSuccess)
+            return bail(e, "cudaMalloc(job table)");
+        if (!jobs.empty() &&
+            (e = cudaMemcpy(b->jobs_dev, jobs.data(), jobs.size() * sizeof(wxk::Job), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return bail(e, "cudaMemcpy(job table)");
+        if ((e = wx::dev_alloc(&b->counter, sizeof(uint32_t))) != cudaSuccess) return bail(e, "cudaMalloc(counter)");
+        // Capture counter reset + persistent launch into a graph, replayed by wx_batch_launch.
+        cudaStream_t cs;
+        if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "cudaStreamCreate");
+        if ((e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+            cudaStreamDestroy(cs);
+            return bail(e, "cudaStreamBeginCapture");
+        }
+        cudaError_t le = b->njobs ? wxk::launch_batched(b->jobs_dev, b->njobs, total, b->counter, ctx->tuning,
+                                                        ctx->num_sms, wxk::all_modes(jobs.data(), jobs.size()), cs)
+                                  : cudaMemsetAsync(b->counter, 0, sizeof(uint32_t), cs);
+        e = cudaStreamEndCapture(cs, &b->graph);
         cudaStreamDestroy(cs);
-        return bail(e, "cudaStreamBeginCapture");
-    }
-    cudaError_t le = b->njobs ? wxk::launch_batched(b->jobs_dev, b->njobs, total, b->counter, ctx->tuning,
-                                                    ctx->num_sms, wxk::all_modes(jobs.data(), jobs.size()), cs)
-                              : cudaMemsetAsync(b->counter, 0, sizeof(uint32_t), cs);
-    e = cudaStreamEndCapture(cs, &b->graph);
-    cudaStreamDestroy(cs);
-    if (le != cudaSuccess) return bail(le, "capture launch_batched");
-    if (e != cudaSuccess) return bail(e, "cudaStreamEndCapture");
-    if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess) return bail(e, "cudaGraphInstantiate");
-    *out = b;
-    return WX_OK;
+        if (le != cudaSuccess) return bail(le, "capture launch_batched");
+        if (e != cudaSuccess) return bail(e, "cudaStreamEndCapture");
+        if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess) return bail(e, "cudaGraphInstantiate");
+        *out = b;
+        return WX_OK;
+    });
 }
 
 int wx_batch_launch(wx_batch *b, void *stream) {

@@ -283,12 +283,14 @@ int wx_state_build(const float eye[3], const float target[3], const float up[3],
 }
 
 int wx_gen_sphere(float cx, float cy, float cz, float radius, float band, wx_topology **out) {
-    if (!out || !(radius >= 0.0f) || !(band > 0.0f)) {
-        set_thread_error("wx_gen_sphere: bad radius/band");
-        return WX_ERR_INVALID;
-    }
-    std::vector<Sphere> s{{{cx, cy, cz}, radius}};
-    return spheres_to_topology(s, band, 0, out);
+    return wx::guard("wx_gen_sphere", [&]() -> int {
+        if (!out || !(radius >= 0.0f) || !(band > 0.0f)) {
+            set_thread_error("wx_gen_sphere: bad radius/band");
+            return WX_ERR_INVALID;
+        }
+        std::vector<Sphere> s{{{cx, cy, cz}, radius}};
+        return spheres_to_topology(s, band, 0, out);
+    });
 }
 
 static std::vector<Sphere> sphere_list(uint32_t count, float rmin, float rmax, float lo, float hi, uint64_t seed) {
@@ -343,12 +345,14 @@ static int spheres_values(const wx_topology *t, const std::vector<Sphere> &sph, 
 
 int wx_gen_sphere_values(const wx_topology *t, float cx, float cy, float cz, float radius, float band,
                          float *values) {
-    if (!t || !values || !(radius >= 0.0f) || !(band > 0.0f)) {
-        set_thread_error("wx_gen_sphere_values: bad arguments");
-        return WX_ERR_INVALID;
-    }
-    std::vector<Sphere> s{{{cx, cy, cz}, radius}};
-    return spheres_values(t, s, band, values);
+    return wx::guard("wx_gen_sphere_values", [&]() -> int {
+        if (!t || !values || !(radius >= 0.0f) || !(band > 0.0f)) {
+            set_thread_error("wx_gen_sphere_values: bad arguments");
+            return WX_ERR_INVALID;
+        }
+        std::vector<Sphere> s{{{cx, cy, cz}, radius}};
+        return spheres_values(t, s, band, values);
+    });
 }
 
 int wx_gen_spheres_values(const wx_topology *t, uint32_t count, float rmin, float rmax, float lo, float hi,

@@ -303,18 +303,6 @@ int sfail(int code, const std::string &msg) {
     wx::set_thread_error(msg);
     return code;
 }
-// Runs an entry point's body so that no exception crosses the C ABI: a failed host
-// allocation is WX_ERR_OOM.
-template <class F>
-int guarded(const char *who, F &&f) {
-    try {
-        return f();
-    } catch (const std::bad_alloc &) {
-        return sfail(WX_ERR_OOM, std::string(who) + ": host allocation failed");
-    } catch (...) {
-        return sfail(WX_ERR_INVALID, std::string(who) + ": unexpected error");
-    }
-}
 void fill_result(const Req *q, wx_result *o) {
     o->ticket = q->ticket;
     o->user = q->r.user;
@@ -332,7 +320,7 @@ void fill_result(const Req *q, wx_result *o) {
 extern "C" {
 
 int wx_server_create(wx_ctx *ctx, const wx_server_config *cfg, wx_server **out) {
-    return guarded("wx_server_create", [&]() -> int {
+    return wx::guard("wx_server_create", [&]() -> int {
         if (!ctx || !cfg || !out) return sfail(WX_ERR_INVALID, "wx_server_create: null argument");
         wx_server_config c = *cfg;
         if (c.max_inflight == 0) c.max_inflight = 2;
@@ -390,7 +378,7 @@ int wx_server_create(wx_ctx *ctx, const wx_server_config *cfg, wx_server **out) 
 }
 
 int wx_server_add_grid(wx_server *s, const wx_grid *grid, uint32_t *grid_id) {
-    return guarded("wx_server_add_grid", [&]() -> int {
+    return wx::guard("wx_server_add_grid", [&]() -> int {
         if (!s || !grid || !grid_id) return sfail(WX_ERR_INVALID, "wx_server_add_grid: null argument");
         wxk::DevGrid g;
         int dev = -1;
@@ -410,7 +398,7 @@ int wx_server_add_grid(wx_server *s, const wx_grid *grid, uint32_t *grid_id) {
 }
 
 int wx_server_submit(wx_server *s, const wx_request *r, uint64_t *ticket) {
-    return guarded("wx_server_submit", [&]() -> int {
+    return wx::guard("wx_server_submit", [&]() -> int {
         if (!s || !r) return sfail(WX_ERR_INVALID, "wx_server_submit: null argument");
         if ((uint64_t)r->width * r->height >= (1ull << 32)) return sfail(WX_ERR_UNSUPPORTED, "wx_server_submit: too large");
         auto *q = new (std::nothrow) Req();
@@ -474,7 +462,7 @@ int wx_server_submit(wx_server *s, const wx_request *r, uint64_t *ticket) {
 }
 
 int wx_server_cancel(wx_server *s, uint64_t ticket) {
-    return guarded("wx_server_cancel", [&]() -> int {
+    return wx::guard("wx_server_cancel", [&]() -> int {
         if (!s) return WX_ERR_INVALID;
         std::lock_guard<std::mutex> lk(s->mu);
         auto it = s->reqs.find(ticket);
@@ -508,7 +496,7 @@ int wx_server_cancel(wx_server *s, uint64_t ticket) {
 }
 
 int wx_server_poll(wx_server *s, wx_result *out, uint32_t max, uint32_t *n, int wait_ms) {
-    return guarded("wx_server_poll", [&]() -> int {
+    return wx::guard("wx_server_poll", [&]() -> int {
         if (!s || !n || (max && !out)) return sfail(WX_ERR_INVALID, "wx_server_poll: null argument");
         std::unique_lock<std::mutex> lk(s->mu);
         if (s->done_q.empty() && wait_ms > 0)
@@ -526,7 +514,7 @@ int wx_server_poll(wx_server *s, wx_result *out, uint32_t max, uint32_t *n, int 
 }
 
 int wx_server_copy_result(wx_server *s, uint64_t ticket, uint8_t *rgba8_host, wx_hit *hits_host) {
-    return guarded("wx_server_copy_result", [&]() -> int {
+    return wx::guard("wx_server_copy_result", [&]() -> int {
         if (!s) return WX_ERR_INVALID;
         const Req *q;
         {
@@ -550,7 +538,7 @@ int wx_server_copy_result(wx_server *s, uint64_t ticket, uint8_t *rgba8_host, wx
 }
 
 int wx_server_release(wx_server *s, uint64_t ticket) {
-    return guarded("wx_server_release", [&]() -> int {
+    return wx::guard("wx_server_release", [&]() -> int {
         if (!s) return WX_ERR_INVALID;
         std::lock_guard<std::mutex> lk(s->mu);
         auto it = s->reqs.find(ticket);
@@ -566,7 +554,7 @@ int wx_server_release(wx_server *s, uint64_t ticket) {
 }
 
 int wx_server_get_stats(wx_server *s, wx_server_stats *o) {
-    return guarded("wx_server_get_stats", [&]() -> int {
+    return wx::guard("wx_server_get_stats", [&]() -> int {
         if (!s || !o) return WX_ERR_INVALID;
         std::lock_guard<std::mutex> lk(s->mu);
         *o = s->st;
@@ -581,7 +569,7 @@ int wx_server_get_stats(wx_server *s, wx_server_stats *o) {
 
 int wx_server_replay(wx_server *s, const wx_request *reqs, const double *arrival_s, uint32_t n, wx_result *results,
                      int release, double timeout_s) {
-    return guarded("wx_server_replay", [&]() -> int {
+    return wx::guard("wx_server_replay", [&]() -> int {
         if (!s || (n && (!reqs || !arrival_s || !results))) return sfail(WX_ERR_INVALID, "wx_server_replay: null argument");
         std::unordered_map<uint64_t, uint32_t> index;
         index.reserve(n * 2);
@@ -628,7 +616,7 @@ int wx_server_replay(wx_server *s, const wx_request *reqs, const double *arrival
 }
 
 int wx_server_destroy(wx_server *s) {
-    return guarded("wx_server_destroy", [&]() -> int {
+    return wx::guard("wx_server_destroy", [&]() -> int {
         if (!s) return WX_OK;
         {
             std::lock_guard<std::mutex> lk(s->mu);

@@ -267,142 +267,148 @@ int wx_topology_from_masks(const uint32_t *kids5, const uint32_t *vals5, uint64_
                            const uint32_t *kids4, const uint32_t *vals4, uint64_t n4,
                            const uint32_t *vals3, uint64_t n3, const int32_t *origins,
                            uint32_t origin_stride, wx_topology **out) {
-    if (!out || (n5 && (!kids5 || !vals5 || !origins)) || (n4 && (!kids4 || !vals4)) ||
-        (n3 && !vals3) || origin_stride < 3) {
-        set_thread_error("wx_topology_from_masks: null pointer or origin_stride < 3");
-        return WX_ERR_INVALID;
-    }
-    auto *t = new (std::nothrow) wx_topology();
-    if (!t) return WX_ERR_OOM;
-    auto w2u = [](const uint32_t *w, size_t nwords64, std::vector<uint64_t> &dst) {
-        dst.resize(nwords64);
-        for (size_t i = 0; i < nwords64; i++) dst[i] = (uint64_t)w[2 * i] | ((uint64_t)w[2 * i + 1] << 32);
-    };
-    t->o5.resize(n5);
-    for (uint64_t i = 0; i < n5; i++) {
-        for (int a = 0; a < 3; a++) t->o5[i][a] = origins[i * origin_stride + a];
-        for (int a = 0; a < 3; a++)
-            if (node_origin(t->o5[i][a], kN5Total) != t->o5[i][a]) {
-                delete t;
-                set_thread_error("wx_topology_from_masks: origin not 4096-aligned");
-                return WX_ERR_INVALID;
-            }
-        if (i && !(t->o5[i - 1] < t->o5[i])) {
-            delete t;
-            set_thread_error("wx_topology_from_masks: origins not strictly ascending");
+    return wx::guard("wx_topology_from_masks", [&]() -> int {
+        if (!out || (n5 && (!kids5 || !vals5 || !origins)) || (n4 && (!kids4 || !vals4)) ||
+            (n3 && !vals3) || origin_stride < 3) {
+            set_thread_error("wx_topology_from_masks: null pointer or origin_stride < 3");
             return WX_ERR_INVALID;
         }
-    }
-    w2u(kids5, n5 * kN5Words, t->kid5);
-    w2u(vals5, n5 * kN5Words, t->val5);
-    w2u(kids4, n4 * kN4Words, t->kid4);
-    w2u(vals4, n4 * kN4Words, t->val4);
-    w2u(vals3, n3 * kN3Words, t->val3);
-    t->derive();
-    if (t->o4.size() != n4 || t->o3.size() != n3) {
-        char msg[160];
-        snprintf(msg, sizeof msg,
-                 "wx_topology_from_masks: child masks name %zu N4 / %zu N3 nodes, view has %llu / %llu",
-                 t->o4.size(), t->o3.size(), (unsigned long long)n4, (unsigned long long)n3);
-        delete t;
-        set_thread_error(msg);
-        return WX_ERR_INVALID;
-    }
-    *out = t;
-    return WX_OK;
+        auto *t = new (std::nothrow) wx_topology();
+        if (!t) return WX_ERR_OOM;
+        auto w2u = [](const uint32_t *w, size_t nwords64, std::vector<uint64_t> &dst) {
+            dst.resize(nwords64);
+            for (size_t i = 0; i < nwords64; i++) dst[i] = (uint64_t)w[2 * i] | ((uint64_t)w[2 * i + 1] << 32);
+        };
+        t->o5.resize(n5);
+        for (uint64_t i = 0; i < n5; i++) {
+            for (int a = 0; a < 3; a++) t->o5[i][a] = origins[i * origin_stride + a];
+            for (int a = 0; a < 3; a++)
+                if (node_origin(t->o5[i][a], kN5Total) != t->o5[i][a]) {
+                    delete t;
+                    set_thread_error("wx_topology_from_masks: origin not 4096-aligned");
+                    return WX_ERR_INVALID;
+                }
+            if (i && !(t->o5[i - 1] < t->o5[i])) {
+                delete t;
+                set_thread_error("wx_topology_from_masks: origins not strictly ascending");
+                return WX_ERR_INVALID;
+            }
+        }
+        w2u(kids5, n5 * kN5Words, t->kid5);
+        w2u(vals5, n5 * kN5Words, t->val5);
+        w2u(kids4, n4 * kN4Words, t->kid4);
+        w2u(vals4, n4 * kN4Words, t->val4);
+        w2u(vals3, n3 * kN3Words, t->val3);
+        t->derive();
+        if (t->o4.size() != n4 || t->o3.size() != n3) {
+            char msg[160];
+            snprintf(msg, sizeof msg,
+                     "wx_topology_from_masks: child masks name %zu N4 / %zu N3 nodes, view has %llu / %llu",
+                     t->o4.size(), t->o3.size(), (unsigned long long)n4, (unsigned long long)n3);
+            delete t;
+            set_thread_error(msg);
+            return WX_ERR_INVALID;
+        }
+        *out = t;
+        return WX_OK;
+    });
 }
 
 int wx_topology_from_leaves(const int32_t *origins, const uint64_t *masks, uint64_t n,
                             wx_topology **out) {
-    if (!out || (n && (!origins || !masks))) {
-        set_thread_error("wx_topology_from_leaves: null pointer");
-        return WX_ERR_INVALID;
-    }
-    struct Leaf {
-        I3 o;
-        uint64_t m[8];
-    };
-    std::vector<Leaf> leaves(n);
-    for (uint64_t i = 0; i < n; i++) {
-        for (int a = 0; a < 3; a++) {
-            leaves[i].o[a] = origins[3 * i + a];
-            if (node_origin(leaves[i].o[a], kN3Total) != leaves[i].o[a]) {
-                set_thread_error("wx_topology_from_leaves: leaf origin not 8-aligned");
-                return WX_ERR_INVALID;
+    return wx::guard("wx_topology_from_leaves", [&]() -> int {
+        if (!out || (n && (!origins || !masks))) {
+            set_thread_error("wx_topology_from_leaves: null pointer");
+            return WX_ERR_INVALID;
+        }
+        struct Leaf {
+            I3 o;
+            uint64_t m[8];
+        };
+        std::vector<Leaf> leaves(n);
+        for (uint64_t i = 0; i < n; i++) {
+            for (int a = 0; a < 3; a++) {
+                leaves[i].o[a] = origins[3 * i + a];
+                if (node_origin(leaves[i].o[a], kN3Total) != leaves[i].o[a]) {
+                    set_thread_error("wx_topology_from_leaves: leaf origin not 8-aligned");
+                    return WX_ERR_INVALID;
+                }
             }
+            memcpy(leaves[i].m, masks + 8 * i, 64);
         }
-        memcpy(leaves[i].m, masks + 8 * i, 64);
-    }
-    // DFS order: N5 key (lexicographic), then N5 slot offset, then N4 slot offset.
-    auto key = [](const I3 &o) {
-        struct K {
-            I3 k5;
-            uint32_t s5, s4;
-        } k;
-        for (int a = 0; a < 3; a++) k.k5[a] = node_origin(o[a], kN5Total);
-        k.s5 = slot_offset(o[0], o[1], o[2], kN5Log2, kN5Total);
-        k.s4 = slot_offset(o[0], o[1], o[2], kN4Log2, kN4Total);
-        return k;
-    };
-    std::sort(leaves.begin(), leaves.end(), [&](const Leaf &a, const Leaf &b) {
-        auto ka = key(a.o), kb = key(b.o);
-        if (ka.k5 != kb.k5) return ka.k5 < kb.k5;
-        if (ka.s5 != kb.s5) return ka.s5 < kb.s5;
-        return ka.s4 < kb.s4;
+        // DFS order: N5 key (lexicographic), then N5 slot offset, then N4 slot offset.
+        auto key = [](const I3 &o) {
+            struct K {
+                I3 k5;
+                uint32_t s5, s4;
+            } k;
+            for (int a = 0; a < 3; a++) k.k5[a] = node_origin(o[a], kN5Total);
+            k.s5 = slot_offset(o[0], o[1], o[2], kN5Log2, kN5Total);
+            k.s4 = slot_offset(o[0], o[1], o[2], kN4Log2, kN4Total);
+            return k;
+        };
+        std::sort(leaves.begin(), leaves.end(), [&](const Leaf &a, const Leaf &b) {
+            auto ka = key(a.o), kb = key(b.o);
+            if (ka.k5 != kb.k5) return ka.k5 < kb.k5;
+            if (ka.s5 != kb.s5) return ka.s5 < kb.s5;
+            return ka.s4 < kb.s4;
+        });
+        auto *t = new (std::nothrow) wx_topology();
+        if (!t) return WX_ERR_OOM;
+        size_t i = 0;
+        while (i < leaves.size()) {
+            auto k = key(leaves[i].o);
+            if (t->o5.empty() || t->o5.back() != k.k5) {
+                t->o5.push_back(k.k5);
+                t->kid5.resize(t->kid5.size() + kN5Words, 0);
+                t->val5.resize(t->val5.size() + kN5Words, 0);
+            }
+            uint64_t *k5 = &t->kid5[(t->o5.size() - 1) * kN5Words];
+            if (!test_bit(k5, k.s5)) {
+                k5[k.s5 >> 6] |= 1ull << (k.s5 & 63);
+                t->kid4.resize(t->kid4.size() + kN4Words, 0);
+                t->val4.resize(t->val4.size() + kN4Words, 0);
+            }
+            uint64_t *k4 = &t->kid4[t->kid4.size() - kN4Words];
+            uint64_t m[8] = {0};
+            size_t j = i;
+            while (j < leaves.size() && leaves[j].o == leaves[i].o) {  // merge duplicates
+                for (int w = 0; w < 8; w++) m[w] |= leaves[j].m[w];
+                j++;
+            }
+            k4[k.s4 >> 6] |= 1ull << (k.s4 & 63);
+            t->val3.insert(t->val3.end(), m, m + 8);
+            i = j;
+        }
+        t->derive();
+        *out = t;
+        return WX_OK;
     });
-    auto *t = new (std::nothrow) wx_topology();
-    if (!t) return WX_ERR_OOM;
-    size_t i = 0;
-    while (i < leaves.size()) {
-        auto k = key(leaves[i].o);
-        if (t->o5.empty() || t->o5.back() != k.k5) {
-            t->o5.push_back(k.k5);
-            t->kid5.resize(t->kid5.size() + kN5Words, 0);
-            t->val5.resize(t->val5.size() + kN5Words, 0);
-        }
-        uint64_t *k5 = &t->kid5[(t->o5.size() - 1) * kN5Words];
-        if (!test_bit(k5, k.s5)) {
-            k5[k.s5 >> 6] |= 1ull << (k.s5 & 63);
-            t->kid4.resize(t->kid4.size() + kN4Words, 0);
-            t->val4.resize(t->val4.size() + kN4Words, 0);
-        }
-        uint64_t *k4 = &t->kid4[t->kid4.size() - kN4Words];
-        uint64_t m[8] = {0};
-        size_t j = i;
-        while (j < leaves.size() && leaves[j].o == leaves[i].o) {  // merge duplicates
-            for (int w = 0; w < 8; w++) m[w] |= leaves[j].m[w];
-            j++;
-        }
-        k4[k.s4 >> 6] |= 1ull << (k.s4 & 63);
-        t->val3.insert(t->val3.end(), m, m + 8);
-        i = j;
-    }
-    t->derive();
-    *out = t;
-    return WX_OK;
 }
 
 int wx_topology_from_voxels(const int32_t *ijk, uint64_t n, wx_topology **out) {
-    if (!out || (n && !ijk)) {
-        set_thread_error("wx_topology_from_voxels: null pointer");
-        return WX_ERR_INVALID;
-    }
-    std::vector<std::pair<I3, uint32_t>> v(n);
-    for (uint64_t i = 0; i < n; i++) {
-        I3 o{node_origin(ijk[3 * i], 3), node_origin(ijk[3 * i + 1], 3), node_origin(ijk[3 * i + 2], 3)};
-        v[i] = {o, slot_offset(ijk[3 * i], ijk[3 * i + 1], ijk[3 * i + 2], kN3Log2, kN3Total)};
-    }
-    std::sort(v.begin(), v.end());
-    std::vector<int32_t> org;
-    std::vector<uint64_t> masks;
-    for (size_t i = 0; i < v.size(); i++) {
-        if (i == 0 || v[i].first != v[i - 1].first) {
-            org.insert(org.end(), v[i].first.begin(), v[i].first.end());
-            masks.resize(masks.size() + 8, 0);
+    return wx::guard("wx_topology_from_voxels", [&]() -> int {
+        if (!out || (n && !ijk)) {
+            set_thread_error("wx_topology_from_voxels: null pointer");
+            return WX_ERR_INVALID;
         }
-        masks[masks.size() - 8 + (v[i].second >> 6)] |= 1ull << (v[i].second & 63);
-    }
-    return wx_topology_from_leaves(org.data(), masks.data(), org.size() / 3, out);
+        std::vector<std::pair<I3, uint32_t>> v(n);
+        for (uint64_t i = 0; i < n; i++) {
+            I3 o{node_origin(ijk[3 * i], 3), node_origin(ijk[3 * i + 1], 3), node_origin(ijk[3 * i + 2], 3)};
+            v[i] = {o, slot_offset(ijk[3 * i], ijk[3 * i + 1], ijk[3 * i + 2], kN3Log2, kN3Total)};
+        }
+        std::sort(v.begin(), v.end());
+        std::vector<int32_t> org;
+        std::vector<uint64_t> masks;
+        for (size_t i = 0; i < v.size(); i++) {
+            if (i == 0 || v[i].first != v[i - 1].first) {
+                org.insert(org.end(), v[i].first.begin(), v[i].first.end());
+                masks.resize(masks.size() + 8, 0);
+            }
+            masks[masks.size() - 8 + (v[i].second >> 6)] |= 1ull << (v[i].second & 63);
+        }
+        return wx_topology_from_leaves(org.data(), masks.data(), org.size() / 3, out);
+    });
 }
 
 void wx_topology_free(wx_topology *topo) { delete topo; }
@@ -424,25 +430,27 @@ uint64_t wx_topology_active_voxels(const wx_topology *t) {
 
 int wx_topology_masks(const wx_topology *t, uint32_t *kids5, uint32_t *vals5, uint32_t *kids4,
                       uint32_t *vals4, uint32_t *vals3, int32_t *origins) {
-    if (!t) return WX_ERR_INVALID;
-    auto u2w = [](const std::vector<uint64_t> &src, uint32_t *dst) {  // arr32_from_arr64
-        if (!dst) return;
-        for (size_t i = 0; i < src.size(); i++) {
-            dst[2 * i] = (uint32_t)src[i];
-            dst[2 * i + 1] = (uint32_t)(src[i] >> 32);
-        }
-    };
-    u2w(t->kid5, kids5);
-    u2w(t->val5, vals5);
-    u2w(t->kid4, kids4);
-    u2w(t->val4, vals4);
-    u2w(t->val3, vals3);
-    if (origins)
-        for (size_t i = 0; i < t->o5.size(); i++) {
-            for (int a = 0; a < 3; a++) origins[4 * i + a] = t->o5[i][a];
-            origins[4 * i + 3] = 0;
-        }
-    return WX_OK;
+    return wx::guard("wx_topology_masks", [&]() -> int {
+        if (!t) return WX_ERR_INVALID;
+        auto u2w = [](const std::vector<uint64_t> &src, uint32_t *dst) {  // arr32_from_arr64
+            if (!dst) return;
+            for (size_t i = 0; i < src.size(); i++) {
+                dst[2 * i] = (uint32_t)src[i];
+                dst[2 * i + 1] = (uint32_t)(src[i] >> 32);
+            }
+        };
+        u2w(t->kid5, kids5);
+        u2w(t->val5, vals5);
+        u2w(t->kid4, kids4);
+        u2w(t->val4, vals4);
+        u2w(t->val3, vals3);
+        if (origins)
+            for (size_t i = 0; i < t->o5.size(); i++) {
+                for (int a = 0; a < 3; a++) origins[4 * i + a] = t->o5[i][a];
+                origins[4 * i + 3] = 0;
+            }
+        return WX_OK;
+    });
 }
 
 int wx_topology_sdf(wx_topology *t, int nthreads) {

@@ -395,15 +395,7 @@ int parse(const char *path, const char *grid_name, wx_topology **out, wx_vdb_inf
 // while reading is WX_ERR_OOM).
 int parse_guarded(const char *path, const char *grid_name, wx_topology **out, wx_vdb_info *info,
                   std::vector<float> *values, float *bg_out, const char *who) {
-    try {
-        return parse(path, grid_name, out, info, values, bg_out, who);
-    } catch (const std::bad_alloc &) {
-        wx::set_thread_error(std::string(who) + ": host allocation failed");
-        return WX_ERR_OOM;
-    } catch (...) {
-        wx::set_thread_error(std::string(who) + ": unexpected error while reading");
-        return WX_ERR_INVALID;
-    }
+    return wx::guard(who, [&]() -> int { return parse(path, grid_name, out, info, values, bg_out, who); });
 }
 
 }  // namespace

@@ -3,6 +3,7 @@
 
 #include <array>
 #include <cstdint>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -47,6 +48,28 @@ inline void offset_child(uint32_t off, int log2d, uint32_t c[3]) {
 inline bool test_bit(const uint64_t *w, uint32_t i) { return (w[i >> 6] >> (i & 63)) & 1u; }
 
 void set_thread_error(const std::string &msg);
+
+// Runs an entry point's body so that no C++ exception crosses the C ABI: a failed
+// host allocation is WX_ERR_OOM, anything else WX_ERR_INVALID (the message is kept
+// when it can still be stored).
+template <class F>
+int guard(const char *who, F &&f) noexcept {
+    try {
+        return f();
+    } catch (const std::bad_alloc &) {
+        try {
+            set_thread_error(std::string(who) + ": host allocation failed");
+        } catch (...) {
+        }
+        return WX_ERR_OOM;
+    } catch (...) {
+        try {
+            set_thread_error(std::string(who) + ": unexpected error");
+        } catch (...) {
+        }
+        return WX_ERR_INVALID;
+    }
+}
 
 }  // namespace wx
 
