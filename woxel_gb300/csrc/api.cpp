@@ -413,88 +413,100 @@ const char *wx_status_string(int status) {
 }
 
 int wx_ctx_create(int device, wx_ctx **out) {
-    if (!out) return fail(nullptr, WX_ERR_INVALID, "wx_ctx_create: out is NULL");
-    int n = 0;
-    cudaError_t e = cudaGetDeviceCount(&n);
-    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDeviceCount");
-    if (device < 0 || device >= n) return fail(nullptr, WX_ERR_INVALID, "wx_ctx_create: no such device");
-    WX_CUDA(nullptr, cudaSetDevice(device));
-    auto *c = new (std::nothrow) wx_ctx();
-    if (!c) return fail(nullptr, WX_ERR_OOM, "host allocation failed");
-    c->device = device;
-    auto cleanup = [&](cudaError_t err, const char *what) {
-        wx_ctx_destroy(c);
-        return cuda_fail(nullptr, err, what);
-    };
-    if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
-        return cleanup(e, "cudaDeviceGetAttribute");
-    if ((e = wxk::init_device_tables()) != cudaSuccess) return cleanup(e, "init_device_tables");
-    if ((e = wx::dev_alloc(&c->counters, kCounterSlots * sizeof(uint32_t))) != cudaSuccess)
-        return cleanup(e, "cudaMalloc(counters)");
-    if ((e = cudaMemset(c->counters, 0, kCounterSlots * sizeof(uint32_t))) != cudaSuccess)
-        return cleanup(e, "cudaMemset(counters)");
-    if ((e = wx::dev_alloc(&c->check, 4 * sizeof(unsigned long long))) != cudaSuccess)
-        return cleanup(e, "cudaMalloc(check)");
-    if ((e = cudaEventCreateWithFlags(&c->jobs_done, cudaEventDisableTiming)) != cudaSuccess)
-        return cleanup(e, "cudaEventCreate");
-    *out = c;
-    return WX_OK;
+    return wx::guard("wx_ctx_create", [&]() -> int {
+        if (!out) return fail(nullptr, WX_ERR_INVALID, "wx_ctx_create: out is NULL");
+        int n = 0;
+        cudaError_t e = cudaGetDeviceCount(&n);
+        if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDeviceCount");
+        if (device < 0 || device >= n) return fail(nullptr, WX_ERR_INVALID, "wx_ctx_create: no such device");
+        WX_CUDA(nullptr, cudaSetDevice(device));
+        auto *c = new (std::nothrow) wx_ctx();
+        if (!c) return fail(nullptr, WX_ERR_OOM, "host allocation failed");
+        c->device = device;
+        auto cleanup = [&](cudaError_t err, const char *what) {
+            wx_ctx_destroy(c);
+            return cuda_fail(nullptr, err, what);
+        };
+        if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
+            return cleanup(e, "cudaDeviceGetAttribute");
+        if ((e = wxk::init_device_tables()) != cudaSuccess) return cleanup(e, "init_device_tables");
+        if ((e = wx::dev_alloc(&c->counters, kCounterSlots * sizeof(uint32_t))) != cudaSuccess)
+            return cleanup(e, "cudaMalloc(counters)");
+        if ((e = cudaMemset(c->counters, 0, kCounterSlots * sizeof(uint32_t))) != cudaSuccess)
+            return cleanup(e, "cudaMemset(counters)");
+        if ((e = wx::dev_alloc(&c->check, 4 * sizeof(unsigned long long))) != cudaSuccess)
+            return cleanup(e, "cudaMalloc(check)");
+        if ((e = cudaEventCreateWithFlags(&c->jobs_done, cudaEventDisableTiming)) != cudaSuccess)
+            return cleanup(e, "cudaEventCreate");
+        *out = c;
+        return WX_OK;
+    });
 }
 
 int wx_ctx_destroy(wx_ctx *ctx) {
-    if (!ctx) return WX_OK;
-    cudaSetDevice(ctx->device);
-    if (ctx->jobs_done) {
-        cudaEventSynchronize(ctx->jobs_done);
-        cudaEventDestroy(ctx->jobs_done);
-    }
-    if (ctx->stage) cudaFree(ctx->stage);
-    if (ctx->counters) cudaFree(ctx->counters);
-    if (ctx->check) cudaFree(ctx->check);
-    if (ctx->jobs_dev) cudaFree(ctx->jobs_dev);
-    if (ctx->jobs_host) cudaFreeHost(ctx->jobs_host);
-    delete ctx;
-    return WX_OK;
+    return wx::guard("wx_ctx_destroy", [&]() -> int {
+        if (!ctx) return WX_OK;
+        cudaSetDevice(ctx->device);
+        if (ctx->jobs_done) {
+            cudaEventSynchronize(ctx->jobs_done);
+            cudaEventDestroy(ctx->jobs_done);
+        }
+        if (ctx->stage) cudaFree(ctx->stage);
+        if (ctx->counters) cudaFree(ctx->counters);
+        if (ctx->check) cudaFree(ctx->check);
+        if (ctx->jobs_dev) cudaFree(ctx->jobs_dev);
+        if (ctx->jobs_host) cudaFreeHost(ctx->jobs_host);
+        delete ctx;
+        return WX_OK;
+    });
 }
 
 const char *wx_last_error(const wx_ctx *ctx) { return ctx ? ctx->err.c_str() : wx_thread_last_error(); }
 
 int wx_ctx_set_tuning(wx_ctx *ctx, const wx_tuning *t) {
-    if (!ctx || !t) return fail(ctx, WX_ERR_INVALID, "wx_ctx_set_tuning: null argument");
-    const bool tw_ok = t->tile_width == 4 || t->tile_width == 8 || t->tile_width == 16 || t->tile_width == 32;
-    if (t->kernel < 0 || t->kernel > 1 || t->warps_per_block < 1 || t->warps_per_block > 8 || t->blocks_per_sm < 0 ||
-        t->blocks_per_sm > 64 || !tw_ok || t->tile_order < 0 || t->tile_order > 1 ||
-        !(t->rays_per_lane == 1 || t->rays_per_lane == 2 || t->rays_per_lane == 4 || t->rays_per_lane == 8))
-        return fail(ctx, WX_ERR_INVALID, "wx_ctx_set_tuning: value out of range");
-    ctx->tuning.kernel = t->kernel;
-    ctx->tuning.warps_per_block = t->warps_per_block;
-    ctx->tuning.blocks_per_sm = t->blocks_per_sm;
-    ctx->tuning.tile_w = t->tile_width;
-    ctx->tuning.order = t->tile_order;
-    ctx->tuning.rays = t->rays_per_lane;
-    return WX_OK;
+    return wx::guard("wx_ctx_set_tuning", [&]() -> int {
+        if (!ctx || !t) return fail(ctx, WX_ERR_INVALID, "wx_ctx_set_tuning: null argument");
+        const bool tw_ok = t->tile_width == 4 || t->tile_width == 8 || t->tile_width == 16 || t->tile_width == 32;
+        if (t->kernel < 0 || t->kernel > 1 || t->warps_per_block < 1 || t->warps_per_block > 8 || t->blocks_per_sm < 0 ||
+            t->blocks_per_sm > 64 || !tw_ok || t->tile_order < 0 || t->tile_order > 1 ||
+            !(t->rays_per_lane == 1 || t->rays_per_lane == 2 || t->rays_per_lane == 4 || t->rays_per_lane == 8))
+            return fail(ctx, WX_ERR_INVALID, "wx_ctx_set_tuning: value out of range");
+        ctx->tuning.kernel = t->kernel;
+        ctx->tuning.warps_per_block = t->warps_per_block;
+        ctx->tuning.blocks_per_sm = t->blocks_per_sm;
+        ctx->tuning.tile_w = t->tile_width;
+        ctx->tuning.order = t->tile_order;
+        ctx->tuning.rays = t->rays_per_lane;
+        return WX_OK;
+    });
 }
 
 int wx_inject_alloc_failures(uint32_t count) {
-    wx::g_alloc_failures.store(count, std::memory_order_relaxed);
-    return WX_OK;
+    return wx::guard("wx_inject_alloc_failures", [&]() -> int {
+        wx::g_alloc_failures.store(count, std::memory_order_relaxed);
+        return WX_OK;
+    });
 }
 
 int wx_ctx_set_sdf_wait_limit(wx_ctx *ctx, uint32_t polls) {
-    if (!ctx) return WX_ERR_INVALID;
-    ctx->sdf_spins = polls ? polls : wxk::kSdfSpinLimit;
-    return WX_OK;
+    return wx::guard("wx_ctx_set_sdf_wait_limit", [&]() -> int {
+        if (!ctx) return WX_ERR_INVALID;
+        ctx->sdf_spins = polls ? polls : wxk::kSdfSpinLimit;
+        return WX_OK;
+    });
 }
 
 int wx_ctx_get_tuning(const wx_ctx *ctx, wx_tuning *t) {
-    if (!ctx || !t) return WX_ERR_INVALID;
-    t->kernel = ctx->tuning.kernel;
-    t->warps_per_block = ctx->tuning.warps_per_block;
-    t->blocks_per_sm = ctx->tuning.blocks_per_sm;
-    t->tile_width = ctx->tuning.tile_w;
-    t->tile_order = ctx->tuning.order;
-    t->rays_per_lane = ctx->tuning.rays;
-    return WX_OK;
+    return wx::guard("wx_ctx_get_tuning", [&]() -> int {
+        if (!ctx || !t) return WX_ERR_INVALID;
+        t->kernel = ctx->tuning.kernel;
+        t->warps_per_block = ctx->tuning.warps_per_block;
+        t->blocks_per_sm = ctx->tuning.blocks_per_sm;
+        t->tile_width = ctx->tuning.tile_w;
+        t->tile_order = ctx->tuning.order;
+        t->rays_per_lane = ctx->tuning.rays;
+        return WX_OK;
+    });
 }
 
 int wx_autotune(wx_ctx *ctx, const wx_frame *frames, uint32_t n, const wx_tuning *candidates, uint32_t ncand,
@@ -567,85 +579,91 @@ int wx_autotune(wx_ctx *ctx, const wx_frame *frames, uint32_t n, const wx_tuning
 }
 
 int wx_check_division(wx_ctx *ctx, uint32_t max_m, uint64_t out[3]) {
-    if (!ctx || !out) return fail(ctx, WX_ERR_INVALID, "wx_check_division: null argument");
-    WX_CUDA(ctx, cudaSetDevice(ctx->device));
-    WX_CUDA(ctx, wxk::check_division(max_m, ctx->check, nullptr));
-    unsigned long long h[3];
-    WX_CUDA(ctx, cudaMemcpy(h, ctx->check, sizeof h, cudaMemcpyDeviceToHost));
-    for (int i = 0; i < 3; i++) out[i] = h[i];
-    return WX_OK;
+    return wx::guard("wx_check_division", [&]() -> int {
+        if (!ctx || !out) return fail(ctx, WX_ERR_INVALID, "wx_check_division: null argument");
+        WX_CUDA(ctx, cudaSetDevice(ctx->device));
+        WX_CUDA(ctx, wxk::check_division(max_m, ctx->check, nullptr));
+        unsigned long long h[3];
+        WX_CUDA(ctx, cudaMemcpy(h, ctx->check, sizeof h, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < 3; i++) out[i] = h[i];
+        return WX_OK;
+    });
 }
 
 int wx_bounds_violations(wx_ctx *ctx, uint64_t *count) {
-    if (!ctx || !count) return fail(ctx, WX_ERR_INVALID, "wx_bounds_violations: null argument");
-#ifdef WX_BOUNDS_CHECK
-    WX_CUDA(ctx, cudaSetDevice(ctx->device));
-    WX_CUDA(ctx, cudaDeviceSynchronize());
-    unsigned long long n = 0;
-    WX_CUDA(ctx, wxk::take_bounds_violations(&n));
-    *count = n;
-    return WX_OK;
-#else
-    *count = 0;
-    return fail(ctx, WX_ERR_UNSUPPORTED, "wx_bounds_violations: not a bounds-checked build");
-#endif
+    return wx::guard("wx_bounds_violations", [&]() -> int {
+        if (!ctx || !count) return fail(ctx, WX_ERR_INVALID, "wx_bounds_violations: null argument");
+    #ifdef WX_BOUNDS_CHECK
+        WX_CUDA(ctx, cudaSetDevice(ctx->device));
+        WX_CUDA(ctx, cudaDeviceSynchronize());
+        unsigned long long n = 0;
+        WX_CUDA(ctx, wxk::take_bounds_violations(&n));
+        *count = n;
+        return WX_OK;
+    #else
+        *count = 0;
+        return fail(ctx, WX_ERR_UNSUPPORTED, "wx_bounds_violations: not a bounds-checked build");
+    #endif
+    });
 }
 
 int wx_grid_build(wx_ctx *ctx, wx_topology *t, wx_grid **out) {
-    if (!ctx || !t || !out) return fail(ctx, WX_ERR_INVALID, "wx_grid_build: null argument");
-    WX_CUDA(ctx, cudaSetDevice(ctx->device));
-    int rc = wx_topology_sdf(t, 0);
-    if (rc != WX_OK) return fail(ctx, rc, wx_thread_last_error());
-    const uint64_t n5 = t->n5(), n4 = t->n4(), n3 = t->n3();
-    if (n4 >= wx::kChildFlag || n3 >= wx::kChildFlag)
-        return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_build: more than 2^31 nodes in a level");
-    std::vector<uint32_t> s5, s4;
-    std::vector<int4> o5(std::max<uint64_t>(n5, 1));
-    try {
-        s5.resize(n5 * wx::kN5Slots);
-        s4.resize(n4 * wx::kN4Slots);
-    } catch (...) {
-        return fail(ctx, WX_ERR_OOM, "wx_grid_build: host allocation failed");
-    }
-    bool too_far = false;
-    for (uint64_t i = 0; i < n5; i++) {
-        o5[i] = make_int4(t->o5[i][0], t->o5[i][1], t->o5[i][2], 0);
-        uint32_t next = t->first4[i];
-        for (uint32_t s = 0; s < wx::kN5Slots; s++) {
-            const bool kid = wx::test_bit(&t->kid5[i * wx::kN5Words], s);
-            const bool val = wx::test_bit(&t->val5[i * wx::kN5Words], s);
-            const uint32_t d = t->d5[i * wx::kN5Slots + s];
-            if (kid) {
-                const uint32_t c = next++;
-                s5[i * wx::kN5Slots + s] = val ? 0u : (wx::kChildFlag | c);
-            } else {
-                too_far |= !val && d >= wx::kChildFlag;
-                s5[i * wx::kN5Slots + s] = val ? 0u : d;
+    return wx::guard("wx_grid_build", [&]() -> int {
+        if (!ctx || !t || !out) return fail(ctx, WX_ERR_INVALID, "wx_grid_build: null argument");
+        WX_CUDA(ctx, cudaSetDevice(ctx->device));
+        int rc = wx_topology_sdf(t, 0);
+        if (rc != WX_OK) return fail(ctx, rc, wx_thread_last_error());
+        const uint64_t n5 = t->n5(), n4 = t->n4(), n3 = t->n3();
+        if (n4 >= wx::kChildFlag || n3 >= wx::kChildFlag)
+            return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_build: more than 2^31 nodes in a level");
+        std::vector<uint32_t> s5, s4;
+        std::vector<int4> o5(std::max<uint64_t>(n5, 1));
+        try {
+            s5.resize(n5 * wx::kN5Slots);
+            s4.resize(n4 * wx::kN4Slots);
+        } catch (...) {
+            return fail(ctx, WX_ERR_OOM, "wx_grid_build: host allocation failed");
+        }
+        bool too_far = false;
+        for (uint64_t i = 0; i < n5; i++) {
+            o5[i] = make_int4(t->o5[i][0], t->o5[i][1], t->o5[i][2], 0);
+            uint32_t next = t->first4[i];
+            for (uint32_t s = 0; s < wx::kN5Slots; s++) {
+                const bool kid = wx::test_bit(&t->kid5[i * wx::kN5Words], s);
+                const bool val = wx::test_bit(&t->val5[i * wx::kN5Words], s);
+                const uint32_t d = t->d5[i * wx::kN5Slots + s];
+                if (kid) {
+                    const uint32_t c = next++;
+                    s5[i * wx::kN5Slots + s] = val ? 0u : (wx::kChildFlag | c);
+                } else {
+                    too_far |= !val && d >= wx::kChildFlag;
+                    s5[i * wx::kN5Slots + s] = val ? 0u : d;
+                }
             }
         }
-    }
-    for (uint64_t j = 0; j < n4; j++) {
-        uint32_t next = t->first3[j];
-        for (uint32_t s = 0; s < wx::kN4Slots; s++) {
-            const bool kid = wx::test_bit(&t->kid4[j * wx::kN4Words], s);
-            const bool val = wx::test_bit(&t->val4[j * wx::kN4Words], s);
-            const uint32_t d = t->d4[j * wx::kN4Slots + s];
-            if (kid) {
-                const uint32_t c = next++;
-                s4[j * wx::kN4Slots + s] = val ? 0u : (wx::kChildFlag | c);
-            } else {
-                too_far |= !val && d >= wx::kChildFlag;
-                s4[j * wx::kN4Slots + s] = val ? 0u : d;
+        for (uint64_t j = 0; j < n4; j++) {
+            uint32_t next = t->first3[j];
+            for (uint32_t s = 0; s < wx::kN4Slots; s++) {
+                const bool kid = wx::test_bit(&t->kid4[j * wx::kN4Words], s);
+                const bool val = wx::test_bit(&t->val4[j * wx::kN4Words], s);
+                const uint32_t d = t->d4[j * wx::kN4Slots + s];
+                if (kid) {
+                    const uint32_t c = next++;
+                    s4[j * wx::kN4Slots + s] = val ? 0u : (wx::kChildFlag | c);
+                } else {
+                    too_far |= !val && d >= wx::kChildFlag;
+                    s4[j * wx::kN4Slots + s] = val ? 0u : d;
+                }
             }
         }
-    }
-    if (too_far) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_build: tile distance >= 2^31");
-    wx_grid *gr = nullptr;
-    rc = upload_pools(ctx, o5, s5.data(), s4.data(), t->slot3.data(), n5, n4, n3, &gr);
-    if (rc != WX_OK) return rc;
-    gr->info.active_voxels = wx_topology_active_voxels(t);
-    *out = gr;
-    return WX_OK;
+        if (too_far) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_build: tile distance >= 2^31");
+        wx_grid *gr = nullptr;
+        rc = upload_pools(ctx, o5, s5.data(), s4.data(), t->slot3.data(), n5, n4, n3, &gr);
+        if (rc != WX_OK) return rc;
+        gr->info.active_voxels = wx_topology_active_voxels(t);
+        *out = gr;
+        return WX_OK;
+    });
 }
 
 // The same pools as wx_grid_build, with compute_sdf and the packing on the
@@ -653,350 +671,364 @@ int wx_grid_build(wx_ctx *ctx, wx_topology *t, wx_grid **out) {
 // child-count prefixes; child tables, child origins, neighbour tables, the
 // three sweeps and the packing run on the device.
 int wx_grid_build_gpu(wx_ctx *ctx, const wx_topology *t, wx_grid **out) {
-    if (!ctx || !t || !out) return fail(ctx, WX_ERR_INVALID, "wx_grid_build_gpu: null argument");
-    WX_CUDA(ctx, cudaSetDevice(ctx->device));
-    using namespace wx;
-    const uint64_t n5 = t->n5(), n4 = t->n4(), n3 = t->n3();
-    int rc = check_pool_limits(ctx, n5, n4, n3);
-    if (rc != WX_OK) return rc;
-    if (t->kid5.size() != n5 * kN5Words || t->val5.size() != n5 * kN5Words || t->kid4.size() != n4 * kN4Words ||
-        t->val4.size() != n4 * kN4Words || t->val3.size() != n3 * kN3Words || t->first4.size() != n5 ||
-        t->first3.size() != n4)
-        return fail(ctx, WX_ERR_INVALID, "wx_grid_build_gpu: masks and node counts disagree");
-    std::vector<int4> o5(std::max<uint64_t>(n5, 1));
-    std::vector<uint32_t> pre5, pre4;
-    try {
-        pre5.resize(n5 * kN5Words);
-        pre4.resize(n4 * kN4Words);
-    } catch (...) {
-        return fail(ctx, WX_ERR_OOM, "wx_grid_build_gpu: host allocation failed");
-    }
-    for (uint64_t i = 0; i < n5; i++) {
-        o5[i] = make_int4(t->o5[i][0], t->o5[i][1], t->o5[i][2], 0);
-        if ((o5[i].x & 4095) || (o5[i].y & 4095) || (o5[i].z & 4095))
-            return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_build_gpu: N5 origins must be multiples of 4096");
-    }
-    auto prefix = [](const std::vector<uint64_t> &kid, uint64_t nodes, uint32_t words, std::vector<uint32_t> &pre) {
-        for (uint64_t n = 0; n < nodes; n++) {
-            uint32_t acc = 0;
-            for (uint32_t w = 0; w < words; w++) {
-                pre[n * words + w] = acc;
-                acc += (uint32_t)__builtin_popcountll(kid[n * words + w]);
-            }
+    return wx::guard("wx_grid_build_gpu", [&]() -> int {
+        if (!ctx || !t || !out) return fail(ctx, WX_ERR_INVALID, "wx_grid_build_gpu: null argument");
+        WX_CUDA(ctx, cudaSetDevice(ctx->device));
+        using namespace wx;
+        const uint64_t n5 = t->n5(), n4 = t->n4(), n3 = t->n3();
+        int rc = check_pool_limits(ctx, n5, n4, n3);
+        if (rc != WX_OK) return rc;
+        if (t->kid5.size() != n5 * kN5Words || t->val5.size() != n5 * kN5Words || t->kid4.size() != n4 * kN4Words ||
+            t->val4.size() != n4 * kN4Words || t->val3.size() != n3 * kN3Words || t->first4.size() != n5 ||
+            t->first3.size() != n4)
+            return fail(ctx, WX_ERR_INVALID, "wx_grid_build_gpu: masks and node counts disagree");
+        std::vector<int4> o5(std::max<uint64_t>(n5, 1));
+        std::vector<uint32_t> pre5, pre4;
+        try {
+            pre5.resize(n5 * kN5Words);
+            pre4.resize(n4 * kN4Words);
+        } catch (...) {
+            return fail(ctx, WX_ERR_OOM, "wx_grid_build_gpu: host allocation failed");
         }
-    };
-    prefix(t->kid5, n5, kN5Words, pre5);
-    prefix(t->kid4, n4, kN4Words, pre4);
-    std::vector<int4> root;
-    try {
-        root = root_block(o5, n5);
-    } catch (...) {
-        return fail(ctx, WX_ERR_OOM, "wx_grid_build_gpu: host allocation failed");
-    }
+        for (uint64_t i = 0; i < n5; i++) {
+            o5[i] = make_int4(t->o5[i][0], t->o5[i][1], t->o5[i][2], 0);
+            if ((o5[i].x & 4095) || (o5[i].y & 4095) || (o5[i].z & 4095))
+                return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_build_gpu: N5 origins must be multiples of 4096");
+        }
+        auto prefix = [](const std::vector<uint64_t> &kid, uint64_t nodes, uint32_t words, std::vector<uint32_t> &pre) {
+            for (uint64_t n = 0; n < nodes; n++) {
+                uint32_t acc = 0;
+                for (uint32_t w = 0; w < words; w++) {
+                    pre[n * words + w] = acc;
+                    acc += (uint32_t)__builtin_popcountll(kid[n * words + w]);
+                }
+            }
+        };
+        prefix(t->kid5, n5, kN5Words, pre5);
+        prefix(t->kid4, n4, kN4Words, pre4);
+        std::vector<int4> root;
+        try {
+            root = root_block(o5, n5);
+        } catch (...) {
+            return fail(ctx, WX_ERR_OOM, "wx_grid_build_gpu: host allocation failed");
+        }
 
-    const uint64_t nmax = std::max<uint64_t>({n5, n4, n3, 1});
-    DevBuf kid5, val5, kid4, val4, val3, dpre5, dpre4, first4, first3, droot, c5, c4, org5, org4, org3, d5, d4, d3,
-        nb, indeg, queue, ctr;
-    struct Alloc {
-        DevBuf *b;
-        size_t bytes;
-    } allocs[] = {{&kid5, n5 * kN5Words * 8},  {&val5, n5 * kN5Words * 8}, {&kid4, n4 * kN4Words * 8},
-                  {&val4, n4 * kN4Words * 8},  {&val3, n3 * kN3Words * 8}, {&dpre5, n5 * kN5Words * 4},
-                  {&dpre4, n4 * kN4Words * 4}, {&first4, n5 * 4},          {&first3, n4 * 4},
-                  {&droot, root.size() * 16},  {&c5, n5 * kN5Slots * 4},   {&c4, n4 * kN4Slots * 4},
-                  {&org5, n5 * 16},            {&org4, n4 * 16},           {&org3, n3 * 16},
-                  {&d5, n5 * kN5Slots * 4},    {&d4, n4 * kN4Slots * 4},   {&d3, n3 * kN3Slots * 4},
-                  {&nb, nmax * 27 * 4},        {&indeg, nmax * 4},         {&queue, nmax * 4},
-                  {&ctr, 8 * 4}};
-    for (auto &a : allocs)
-        if (a.bytes) WX_CUDA(ctx, wx::dev_alloc(&a.b->p, a.bytes));
-    struct Up {
-        DevBuf *b;
-        const void *src;
-        size_t bytes;
-    } ups[] = {{&kid5, t->kid5.data(), n5 * kN5Words * 8}, {&val5, t->val5.data(), n5 * kN5Words * 8},
-               {&kid4, t->kid4.data(), n4 * kN4Words * 8}, {&val4, t->val4.data(), n4 * kN4Words * 8},
-               {&val3, t->val3.data(), n3 * kN3Words * 8}, {&dpre5, pre5.data(), n5 * kN5Words * 4},
-               {&dpre4, pre4.data(), n4 * kN4Words * 4},   {&first4, t->first4.data(), n5 * 4},
-               {&first3, t->first3.data(), n4 * 4},        {&droot, root.data(), root.size() * 16},
-               {&org5, o5.data(), n5 * 16}};
-    for (auto &u : ups)
-        if (u.bytes) WX_CUDA(ctx, cudaMemcpy(u.b->p, u.src, u.bytes, cudaMemcpyHostToDevice));
-    const cudaStream_t st = nullptr;
-    WX_CUDA(ctx, cudaMemsetAsync(ctr.p, 0, 8 * 4, st));
-    WX_CUDA(ctx, wxk::sdf_child_table(kid5.as<uint64_t>(), dpre5.as<uint32_t>(), first4.as<uint32_t>(), n5, 15,
-                                      c5.as<uint32_t>(), st));
-    WX_CUDA(ctx, wxk::sdf_child_table(kid4.as<uint64_t>(), dpre4.as<uint32_t>(), first3.as<uint32_t>(), n4, 12,
-                                      c4.as<uint32_t>(), st));
-    WX_CUDA(ctx, wxk::sdf_child_origins(c5.as<uint32_t>(), org5.as<int4>(), n5, 5, 7, org4.as<int4>(), st));
-    WX_CUDA(ctx, wxk::sdf_child_origins(c4.as<uint32_t>(), org4.as<int4>(), n4, 4, 3, org3.as<int4>(), st));
-    WX_CUDA(ctx, wxk::sdf_init(kid5.as<uint64_t>(), n5 * kN5Slots, d5.as<uint32_t>(), st));
-    WX_CUDA(ctx, wxk::sdf_init(kid4.as<uint64_t>(), n4 * kN4Slots, d4.as<uint32_t>(), st));
-    WX_CUDA(ctx, wxk::sdf_init(val3.as<uint64_t>(), n3 * kN3Slots, d3.as<uint32_t>(), st));
-    const wxk::SdfTree tree{droot.as<int4>(), (uint32_t)n5, c5.as<uint32_t>(), c4.as<uint32_t>()};
-    struct Level {
-        int L;
-        DevBuf *org, *d;
-        uint64_t nc;
-    } levels[] = {{5, &org5, &d5, n5}, {4, &org4, &d4, n4}, {3, &org3, &d3, n3}};
-    for (auto &lv : levels) {
-        WX_CUDA(ctx, wxk::sdf_neighbours(lv.L, lv.org->as<int4>(), (uint32_t)lv.nc, tree, nb.as<uint32_t>(), st));
-        WX_CUDA(ctx, wxk::sdf_sweep(lv.L, lv.d->as<uint32_t>(), nb.as<uint32_t>(), (uint32_t)lv.nc,
-                                    indeg.as<uint32_t>(), queue.as<uint32_t>(), ctr.as<uint32_t>(), ctx->num_sms,
-                                    ctx->sdf_spins, st));
-    }
-    // Count the leaf overflow entries (ctr[3]) to size the grid block.
-    uint32_t *flags = ctr.as<uint32_t>();
-    WX_CUDA(ctx, wxk::sdf_pack_leaves(d3.as<uint32_t>(), n3 * kN3Slots, nullptr, nullptr, 0, flags + 3, st));
-    uint32_t h[8];
-    WX_CUDA(ctx, cudaMemcpy(h, flags, sizeof h, cudaMemcpyDeviceToHost));
-    if (h[2]) return fail(ctx, WX_ERR_TIMEOUT, "wx_grid_build_gpu: a sweep's dependency wait hit its bound");
-    const uint64_t n_ovf = h[3];
-    wx_grid *gr = nullptr;
-    if ((rc = alloc_grid(ctx, o5, n5, n4, n3, n_ovf, &gr)) != WX_OK) return rc;
-    cudaError_t e = cudaMemsetAsync(flags + 3, 0, 2 * 4, st);  // ctr[3] overflow count, ctr[4] distance error
-    if (e == cudaSuccess)
-        e = wxk::sdf_pack_internal(kid5.as<uint64_t>(), val5.as<uint64_t>(), c5.as<uint32_t>(), d5.as<uint32_t>(),
-                                   n5 * kN5Slots, const_cast<uint32_t *>(gr->g.slot5), flags + 4, st);
-    if (e == cudaSuccess)
-        e = wxk::sdf_pack_internal(kid4.as<uint64_t>(), val4.as<uint64_t>(), c4.as<uint32_t>(), d4.as<uint32_t>(),
-                                   n4 * kN4Slots, const_cast<uint32_t *>(gr->g.slot4), flags + 4, st);
-    if (e == cudaSuccess)
-        e = wxk::sdf_pack_leaves(d3.as<uint32_t>(), n3 * kN3Slots, const_cast<uint8_t *>(gr->g.leaf),
-                                 const_cast<uint2 *>(gr->g.ovf), (uint32_t)n_ovf, flags + 3, st);
-    if (e == cudaSuccess) e = cudaMemcpy(h, flags, sizeof h, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) {
-        free_grid(gr);
-        return cuda_fail(ctx, e, "wx_grid_build_gpu: packing");
-    }
-    if (h[4]) {
-        free_grid(gr);
-        return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_build_gpu: tile distance >= 2^31");
-    }
-    if (n_ovf) {  // entries arrive in any order; the kernels binary-search them by key
-        std::vector<uint2> ov(n_ovf);
-        e = cudaMemcpy(ov.data(), gr->g.ovf, n_ovf * 8, cudaMemcpyDeviceToHost);
-        std::sort(ov.begin(), ov.end(), [](const uint2 &a, const uint2 &b) { return a.x < b.x; });
-        if (e == cudaSuccess) e = cudaMemcpy((void *)gr->g.ovf, ov.data(), n_ovf * 8, cudaMemcpyHostToDevice);
+        const uint64_t nmax = std::max<uint64_t>({n5, n4, n3, 1});
+        DevBuf kid5, val5, kid4, val4, val3, dpre5, dpre4, first4, first3, droot, c5, c4, org5, org4, org3, d5, d4, d3,
+            nb, indeg, queue, ctr;
+        struct Alloc {
+            DevBuf *b;
+            size_t bytes;
+        } allocs[] = {{&kid5, n5 * kN5Words * 8},  {&val5, n5 * kN5Words * 8}, {&kid4, n4 * kN4Words * 8},
+                      {&val4, n4 * kN4Words * 8},  {&val3, n3 * kN3Words * 8}, {&dpre5, n5 * kN5Words * 4},
+                      {&dpre4, n4 * kN4Words * 4}, {&first4, n5 * 4},          {&first3, n4 * 4},
+                      {&droot, root.size() * 16},  {&c5, n5 * kN5Slots * 4},   {&c4, n4 * kN4Slots * 4},
+                      {&org5, n5 * 16},            {&org4, n4 * 16},           {&org3, n3 * 16},
+                      {&d5, n5 * kN5Slots * 4},    {&d4, n4 * kN4Slots * 4},   {&d3, n3 * kN3Slots * 4},
+                      {&nb, nmax * 27 * 4},        {&indeg, nmax * 4},         {&queue, nmax * 4},
+                      {&ctr, 8 * 4}};
+        for (auto &a : allocs)
+            if (a.bytes) WX_CUDA(ctx, wx::dev_alloc(&a.b->p, a.bytes));
+        struct Up {
+            DevBuf *b;
+            const void *src;
+            size_t bytes;
+        } ups[] = {{&kid5, t->kid5.data(), n5 * kN5Words * 8}, {&val5, t->val5.data(), n5 * kN5Words * 8},
+                   {&kid4, t->kid4.data(), n4 * kN4Words * 8}, {&val4, t->val4.data(), n4 * kN4Words * 8},
+                   {&val3, t->val3.data(), n3 * kN3Words * 8}, {&dpre5, pre5.data(), n5 * kN5Words * 4},
+                   {&dpre4, pre4.data(), n4 * kN4Words * 4},   {&first4, t->first4.data(), n5 * 4},
+                   {&first3, t->first3.data(), n4 * 4},        {&droot, root.data(), root.size() * 16},
+                   {&org5, o5.data(), n5 * 16}};
+        for (auto &u : ups)
+            if (u.bytes) WX_CUDA(ctx, cudaMemcpy(u.b->p, u.src, u.bytes, cudaMemcpyHostToDevice));
+        const cudaStream_t st = nullptr;
+        WX_CUDA(ctx, cudaMemsetAsync(ctr.p, 0, 8 * 4, st));
+        WX_CUDA(ctx, wxk::sdf_child_table(kid5.as<uint64_t>(), dpre5.as<uint32_t>(), first4.as<uint32_t>(), n5, 15,
+                                          c5.as<uint32_t>(), st));
+        WX_CUDA(ctx, wxk::sdf_child_table(kid4.as<uint64_t>(), dpre4.as<uint32_t>(), first3.as<uint32_t>(), n4, 12,
+                                          c4.as<uint32_t>(), st));
+        WX_CUDA(ctx, wxk::sdf_child_origins(c5.as<uint32_t>(), org5.as<int4>(), n5, 5, 7, org4.as<int4>(), st));
+        WX_CUDA(ctx, wxk::sdf_child_origins(c4.as<uint32_t>(), org4.as<int4>(), n4, 4, 3, org3.as<int4>(), st));
+        WX_CUDA(ctx, wxk::sdf_init(kid5.as<uint64_t>(), n5 * kN5Slots, d5.as<uint32_t>(), st));
+        WX_CUDA(ctx, wxk::sdf_init(kid4.as<uint64_t>(), n4 * kN4Slots, d4.as<uint32_t>(), st));
+        WX_CUDA(ctx, wxk::sdf_init(val3.as<uint64_t>(), n3 * kN3Slots, d3.as<uint32_t>(), st));
+        const wxk::SdfTree tree{droot.as<int4>(), (uint32_t)n5, c5.as<uint32_t>(), c4.as<uint32_t>()};
+        struct Level {
+            int L;
+            DevBuf *org, *d;
+            uint64_t nc;
+        } levels[] = {{5, &org5, &d5, n5}, {4, &org4, &d4, n4}, {3, &org3, &d3, n3}};
+        for (auto &lv : levels) {
+            WX_CUDA(ctx, wxk::sdf_neighbours(lv.L, lv.org->as<int4>(), (uint32_t)lv.nc, tree, nb.as<uint32_t>(), st));
+            WX_CUDA(ctx, wxk::sdf_sweep(lv.L, lv.d->as<uint32_t>(), nb.as<uint32_t>(), (uint32_t)lv.nc,
+                                        indeg.as<uint32_t>(), queue.as<uint32_t>(), ctr.as<uint32_t>(), ctx->num_sms,
+                                        ctx->sdf_spins, st));
+        }
+        // Count the leaf overflow entries (ctr[3]) to size the grid block.
+        uint32_t *flags = ctr.as<uint32_t>();
+        WX_CUDA(ctx, wxk::sdf_pack_leaves(d3.as<uint32_t>(), n3 * kN3Slots, nullptr, nullptr, 0, flags + 3, st));
+        uint32_t h[8];
+        WX_CUDA(ctx, cudaMemcpy(h, flags, sizeof h, cudaMemcpyDeviceToHost));
+        if (h[2]) return fail(ctx, WX_ERR_TIMEOUT, "wx_grid_build_gpu: a sweep's dependency wait hit its bound");
+        const uint64_t n_ovf = h[3];
+        wx_grid *gr = nullptr;
+        if ((rc = alloc_grid(ctx, o5, n5, n4, n3, n_ovf, &gr)) != WX_OK) return rc;
+        cudaError_t e = cudaMemsetAsync(flags + 3, 0, 2 * 4, st);  // ctr[3] overflow count, ctr[4] distance error
+        if (e == cudaSuccess)
+            e = wxk::sdf_pack_internal(kid5.as<uint64_t>(), val5.as<uint64_t>(), c5.as<uint32_t>(), d5.as<uint32_t>(),
+                                       n5 * kN5Slots, const_cast<uint32_t *>(gr->g.slot5), flags + 4, st);
+        if (e == cudaSuccess)
+            e = wxk::sdf_pack_internal(kid4.as<uint64_t>(), val4.as<uint64_t>(), c4.as<uint32_t>(), d4.as<uint32_t>(),
+                                       n4 * kN4Slots, const_cast<uint32_t *>(gr->g.slot4), flags + 4, st);
+        if (e == cudaSuccess)
+            e = wxk::sdf_pack_leaves(d3.as<uint32_t>(), n3 * kN3Slots, const_cast<uint8_t *>(gr->g.leaf),
+                                     const_cast<uint2 *>(gr->g.ovf), (uint32_t)n_ovf, flags + 3, st);
+        if (e == cudaSuccess) e = cudaMemcpy(h, flags, sizeof h, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) {
             free_grid(gr);
-            return cuda_fail(ctx, e, "wx_grid_build_gpu: overflow table");
+            return cuda_fail(ctx, e, "wx_grid_build_gpu: packing");
         }
-    }
-    gr->info.active_voxels = wx_topology_active_voxels(t);
-    *out = gr;
-    return WX_OK;
+        if (h[4]) {
+            free_grid(gr);
+            return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_build_gpu: tile distance >= 2^31");
+        }
+        if (n_ovf) {  // entries arrive in any order; the kernels binary-search them by key
+            std::vector<uint2> ov(n_ovf);
+            e = cudaMemcpy(ov.data(), gr->g.ovf, n_ovf * 8, cudaMemcpyDeviceToHost);
+            std::sort(ov.begin(), ov.end(), [](const uint2 &a, const uint2 &b) { return a.x < b.x; });
+            if (e == cudaSuccess) e = cudaMemcpy((void *)gr->g.ovf, ov.data(), n_ovf * 8, cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) {
+                free_grid(gr);
+                return cuda_fail(ctx, e, "wx_grid_build_gpu: overflow table");
+            }
+        }
+        gr->info.active_voxels = wx_topology_active_voxels(t);
+        *out = gr;
+        return WX_OK;
+    });
 }
 
 int wx_grid_read_pools(wx_ctx *ctx, const wx_grid *grid, uint32_t *slot5, uint32_t *slot4, uint8_t *leaf,
                        uint32_t *ovf, uint64_t *n_ovf) {
-    if (!ctx || !grid) return fail(ctx, WX_ERR_INVALID, "wx_grid_read_pools: null argument");
-    WX_CUDA(ctx, cudaSetDevice(grid->device));
-    if (n_ovf) *n_ovf = grid->g.n_ovf;
-    const uint64_t n5 = grid->info.n5, n4 = grid->info.n4, n3 = grid->info.n3;
-    if (slot5 && n5) WX_CUDA(ctx, cudaMemcpy(slot5, grid->g.slot5, n5 * wx::kN5Slots * 4, cudaMemcpyDeviceToHost));
-    if (slot4 && n4) WX_CUDA(ctx, cudaMemcpy(slot4, grid->g.slot4, n4 * wx::kN4Slots * 4, cudaMemcpyDeviceToHost));
-    if (leaf && n3) WX_CUDA(ctx, cudaMemcpy(leaf, grid->g.leaf, n3 * wx::kN3Slots, cudaMemcpyDeviceToHost));
-    if (ovf && grid->g.n_ovf)
-        WX_CUDA(ctx, cudaMemcpy(ovf, grid->g.ovf, (size_t)grid->g.n_ovf * 8, cudaMemcpyDeviceToHost));
-    return WX_OK;
+    return wx::guard("wx_grid_read_pools", [&]() -> int {
+        if (!ctx || !grid) return fail(ctx, WX_ERR_INVALID, "wx_grid_read_pools: null argument");
+        WX_CUDA(ctx, cudaSetDevice(grid->device));
+        if (n_ovf) *n_ovf = grid->g.n_ovf;
+        const uint64_t n5 = grid->info.n5, n4 = grid->info.n4, n3 = grid->info.n3;
+        if (slot5 && n5) WX_CUDA(ctx, cudaMemcpy(slot5, grid->g.slot5, n5 * wx::kN5Slots * 4, cudaMemcpyDeviceToHost));
+        if (slot4 && n4) WX_CUDA(ctx, cudaMemcpy(slot4, grid->g.slot4, n4 * wx::kN4Slots * 4, cudaMemcpyDeviceToHost));
+        if (leaf && n3) WX_CUDA(ctx, cudaMemcpy(leaf, grid->g.leaf, n3 * wx::kN3Slots, cudaMemcpyDeviceToHost));
+        if (ovf && grid->g.n_ovf)
+            WX_CUDA(ctx, cudaMemcpy(ovf, grid->g.ovf, (size_t)grid->g.n_ovf * 8, cudaMemcpyDeviceToHost));
+        return WX_OK;
+    });
 }
 
 int wx_grid_upload(wx_ctx *ctx, const wx_vdb345_view *v, wx_grid **out) {
-    if (!ctx || !v || !out) return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: null argument");
-    if (v->origin_stride < 3) return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: origin_stride < 3");
-    const uint64_t n5 = v->n5, n4 = v->n4, n3 = v->n3;
-    if ((n5 && (!v->kids5 || !v->vals5 || !v->origins || !v->atlas[0])) ||
-        (n4 && (!v->kids4 || !v->vals4 || !v->atlas[1])) || (n3 && (!v->vals3 || !v->atlas[2])))
-        return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: missing mask/atlas arrays");
-    if (n4 >= wx::kChildFlag || n3 >= wx::kChildFlag || n5 >= wx::kChildFlag)
-        return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_upload: more than 2^31 nodes in a level");
-    WX_CUDA(ctx, cudaSetDevice(ctx->device));
-    // Atlas block placement as the shader computes it: dim = textureDimensions
-    // (.y for N5, .x for N4/N3) >> log2(node dim); block (idx%d, (idx/d)%d, idx/d^2).
-    const uint32_t d5 = v->dims[0][1] >> 5, d4 = v->dims[1][0] >> 4, d3 = v->dims[2][0] >> 3;
-    auto block_ok = [&](int lvl, uint64_t n, uint32_t d, uint32_t nd) {
-        if (n == 0) return true;
-        if (d == 0) return false;
-        const uint64_t dd = (uint64_t)d * d;
-        const uint64_t need_x = nd * std::min<uint64_t>(n, d), need_y = nd * std::min<uint64_t>((n + d - 1) / d, d),
-                       need_z = nd * ((n + dd - 1) / dd);
-        return need_x <= v->dims[lvl][0] && need_y <= v->dims[lvl][1] && need_z <= v->dims[lvl][2];
-    };
-    if (!block_ok(0, n5, d5, 32) || !block_ok(1, n4, d4, 16) || !block_ok(2, n3, d3, 8))
-        return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: atlas dimensions too small for the node counts");
-    auto texel = [&](int lvl, uint64_t idx, uint32_t d, uint32_t nd, uint32_t cx, uint32_t cy, uint32_t cz) {
-        const uint64_t x = nd * (idx % d) + cx, y = nd * ((idx / d) % d) + cy, z = nd * (idx / ((uint64_t)d * d)) + cz;
-        return v->atlas[lvl][(z * v->dims[lvl][1] + y) * v->dims[lvl][0] + x];
-    };
-    std::vector<uint32_t> s5, s4, s3;
-    std::vector<int4> o5(std::max<uint64_t>(n5, 1));
-    try {
-        s5.resize(n5 * wx::kN5Slots);
-        s4.resize(n4 * wx::kN4Slots);
-        s3.resize(n3 * wx::kN3Slots);
-    } catch (...) {
-        return fail(ctx, WX_ERR_OOM, "wx_grid_upload: host allocation failed");
-    }
-    std::atomic<int> bad{0};
-    for (uint64_t i = 0; i < n5; i++) {
-        const int32_t *o = v->origins + i * v->origin_stride;
-        o5[i] = make_int4(o[0], o[1], o[2], 0);
-    }
-    parallel_chunks(n5, [&](size_t lo, size_t hi) {
-        for (size_t i = lo; i < hi; i++)
-            for (uint32_t s = 0; s < wx::kN5Slots; s++) {
-                const uint32_t w = s >> 5, b = 1u << (s & 31);
-                const bool kid = v->kids5[i * 1024 + w] & b, val = v->vals5[i * 1024 + w] & b;
-                uint32_t c[3];
-                wx::offset_child(s, 5, c);
-                const uint32_t tx = texel(0, i, d5, 32, c[0], c[1], c[2]);
-                uint32_t word;
-                if (val) word = 0;
-                else if (kid) { word = wx::kChildFlag | tx; if (tx >= n4) bad = 1; }
-                else { word = tx; if (tx >= wx::kChildFlag) bad = 2; }
-                s5[i * wx::kN5Slots + s] = word;
-            }
+    return wx::guard("wx_grid_upload", [&]() -> int {
+        if (!ctx || !v || !out) return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: null argument");
+        if (v->origin_stride < 3) return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: origin_stride < 3");
+        const uint64_t n5 = v->n5, n4 = v->n4, n3 = v->n3;
+        if ((n5 && (!v->kids5 || !v->vals5 || !v->origins || !v->atlas[0])) ||
+            (n4 && (!v->kids4 || !v->vals4 || !v->atlas[1])) || (n3 && (!v->vals3 || !v->atlas[2])))
+            return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: missing mask/atlas arrays");
+        if (n4 >= wx::kChildFlag || n3 >= wx::kChildFlag || n5 >= wx::kChildFlag)
+            return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_upload: more than 2^31 nodes in a level");
+        WX_CUDA(ctx, cudaSetDevice(ctx->device));
+        // Atlas block placement as the shader computes it: dim = textureDimensions
+        // (.y for N5, .x for N4/N3) >> log2(node dim); block (idx%d, (idx/d)%d, idx/d^2).
+        const uint32_t d5 = v->dims[0][1] >> 5, d4 = v->dims[1][0] >> 4, d3 = v->dims[2][0] >> 3;
+        auto block_ok = [&](int lvl, uint64_t n, uint32_t d, uint32_t nd) {
+            if (n == 0) return true;
+            if (d == 0) return false;
+            const uint64_t dd = (uint64_t)d * d;
+            const uint64_t need_x = nd * std::min<uint64_t>(n, d), need_y = nd * std::min<uint64_t>((n + d - 1) / d, d),
+                           need_z = nd * ((n + dd - 1) / dd);
+            return need_x <= v->dims[lvl][0] && need_y <= v->dims[lvl][1] && need_z <= v->dims[lvl][2];
+        };
+        if (!block_ok(0, n5, d5, 32) || !block_ok(1, n4, d4, 16) || !block_ok(2, n3, d3, 8))
+            return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: atlas dimensions too small for the node counts");
+        auto texel = [&](int lvl, uint64_t idx, uint32_t d, uint32_t nd, uint32_t cx, uint32_t cy, uint32_t cz) {
+            const uint64_t x = nd * (idx % d) + cx, y = nd * ((idx / d) % d) + cy, z = nd * (idx / ((uint64_t)d * d)) + cz;
+            return v->atlas[lvl][(z * v->dims[lvl][1] + y) * v->dims[lvl][0] + x];
+        };
+        std::vector<uint32_t> s5, s4, s3;
+        std::vector<int4> o5(std::max<uint64_t>(n5, 1));
+        try {
+            s5.resize(n5 * wx::kN5Slots);
+            s4.resize(n4 * wx::kN4Slots);
+            s3.resize(n3 * wx::kN3Slots);
+        } catch (...) {
+            return fail(ctx, WX_ERR_OOM, "wx_grid_upload: host allocation failed");
+        }
+        std::atomic<int> bad{0};
+        for (uint64_t i = 0; i < n5; i++) {
+            const int32_t *o = v->origins + i * v->origin_stride;
+            o5[i] = make_int4(o[0], o[1], o[2], 0);
+        }
+        parallel_chunks(n5, [&](size_t lo, size_t hi) {
+            for (size_t i = lo; i < hi; i++)
+                for (uint32_t s = 0; s < wx::kN5Slots; s++) {
+                    const uint32_t w = s >> 5, b = 1u << (s & 31);
+                    const bool kid = v->kids5[i * 1024 + w] & b, val = v->vals5[i * 1024 + w] & b;
+                    uint32_t c[3];
+                    wx::offset_child(s, 5, c);
+                    const uint32_t tx = texel(0, i, d5, 32, c[0], c[1], c[2]);
+                    uint32_t word;
+                    if (val) word = 0;
+                    else if (kid) { word = wx::kChildFlag | tx; if (tx >= n4) bad = 1; }
+                    else { word = tx; if (tx >= wx::kChildFlag) bad = 2; }
+                    s5[i * wx::kN5Slots + s] = word;
+                }
+        });
+        parallel_chunks(n4, [&](size_t lo, size_t hi) {
+            for (size_t j = lo; j < hi; j++)
+                for (uint32_t s = 0; s < wx::kN4Slots; s++) {
+                    const uint32_t w = s >> 5, b = 1u << (s & 31);
+                    const bool kid = v->kids4[j * 128 + w] & b, val = v->vals4[j * 128 + w] & b;
+                    uint32_t c[3];
+                    wx::offset_child(s, 4, c);
+                    const uint32_t tx = texel(1, j, d4, 16, c[0], c[1], c[2]);
+                    uint32_t word;
+                    if (val) word = 0;
+                    else if (kid) { word = wx::kChildFlag | tx; if (tx >= n3) bad = 1; }
+                    else { word = tx; if (tx >= wx::kChildFlag) bad = 2; }
+                    s4[j * wx::kN4Slots + s] = word;
+                }
+        });
+        parallel_chunks(n3, [&](size_t lo, size_t hi) {
+            for (size_t k = lo; k < hi; k++)
+                for (uint32_t s = 0; s < wx::kN3Slots; s++) {
+                    const bool val = v->vals3[k * 16 + (s >> 5)] & (1u << (s & 31));
+                    uint32_t c[3];
+                    wx::offset_child(s, 3, c);
+                    s3[k * wx::kN3Slots + s] = val ? 0u : texel(2, k, d3, 8, c[0], c[1], c[2]);
+                }
+        });
+        if (bad == 1) return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: child index in atlas out of range");
+        if (bad == 2) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_upload: internal tile distance >= 2^31");
+        wx_grid *gr = nullptr;
+        int rc = upload_pools(ctx, o5, s5.data(), s4.data(), s3.data(), n5, n4, n3, &gr);
+        if (rc != WX_OK) return rc;
+        uint64_t act = 0;
+        for (uint64_t w = 0; w < n3 * 16; w++) act += (uint64_t)__builtin_popcount(v->vals3[w]);
+        gr->info.active_voxels = act;
+        *out = gr;
+        return WX_OK;
     });
-    parallel_chunks(n4, [&](size_t lo, size_t hi) {
-        for (size_t j = lo; j < hi; j++)
-            for (uint32_t s = 0; s < wx::kN4Slots; s++) {
-                const uint32_t w = s >> 5, b = 1u << (s & 31);
-                const bool kid = v->kids4[j * 128 + w] & b, val = v->vals4[j * 128 + w] & b;
-                uint32_t c[3];
-                wx::offset_child(s, 4, c);
-                const uint32_t tx = texel(1, j, d4, 16, c[0], c[1], c[2]);
-                uint32_t word;
-                if (val) word = 0;
-                else if (kid) { word = wx::kChildFlag | tx; if (tx >= n3) bad = 1; }
-                else { word = tx; if (tx >= wx::kChildFlag) bad = 2; }
-                s4[j * wx::kN4Slots + s] = word;
-            }
-    });
-    parallel_chunks(n3, [&](size_t lo, size_t hi) {
-        for (size_t k = lo; k < hi; k++)
-            for (uint32_t s = 0; s < wx::kN3Slots; s++) {
-                const bool val = v->vals3[k * 16 + (s >> 5)] & (1u << (s & 31));
-                uint32_t c[3];
-                wx::offset_child(s, 3, c);
-                s3[k * wx::kN3Slots + s] = val ? 0u : texel(2, k, d3, 8, c[0], c[1], c[2]);
-            }
-    });
-    if (bad == 1) return fail(ctx, WX_ERR_INVALID, "wx_grid_upload: child index in atlas out of range");
-    if (bad == 2) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_grid_upload: internal tile distance >= 2^31");
-    wx_grid *gr = nullptr;
-    int rc = upload_pools(ctx, o5, s5.data(), s4.data(), s3.data(), n5, n4, n3, &gr);
-    if (rc != WX_OK) return rc;
-    uint64_t act = 0;
-    for (uint64_t w = 0; w < n3 * 16; w++) act += (uint64_t)__builtin_popcount(v->vals3[w]);
-    gr->info.active_voxels = act;
-    *out = gr;
-    return WX_OK;
 }
 
 int wx_grid_release(wx_ctx *ctx, wx_grid *grid) {
-    if (!grid) return WX_OK;
-    cudaSetDevice(grid->device);
-    cudaError_t e = cudaFree(grid->dev);
-    if (grid->values) {
-        const cudaError_t e2 = cudaFree(grid->values);
-        if (e == cudaSuccess) e = e2;
-    }
-    delete grid;
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaFree(node pools)");
-    return WX_OK;
+    return wx::guard("wx_grid_release", [&]() -> int {
+        if (!grid) return WX_OK;
+        cudaSetDevice(grid->device);
+        cudaError_t e = cudaFree(grid->dev);
+        if (grid->values) {
+            const cudaError_t e2 = cudaFree(grid->values);
+            if (e == cudaSuccess) e = e2;
+        }
+        delete grid;
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaFree(node pools)");
+        return WX_OK;
+    });
 }
 
 int wx_grid_set_values(wx_ctx *ctx, wx_grid *grid, const float *values, float band) {
-    if (!ctx || !grid || !values) return fail(ctx, WX_ERR_INVALID, "wx_grid_set_values: null argument");
-    if (!(band > 0.0f) || !(band < 3.0e38f))
-        return fail(ctx, WX_ERR_INVALID, "wx_grid_set_values: band must be positive and finite");
-    WX_CUDA(ctx, cudaSetDevice(grid->device));
-    const size_t bytes = (size_t)grid->info.n3 * wx::kN3Slots * sizeof(float);
-    if (!grid->values && bytes) WX_CUDA(ctx, wx::dev_alloc(&grid->values, bytes));
-    if (bytes) WX_CUDA(ctx, cudaMemcpy(grid->values, values, bytes, cudaMemcpyHostToDevice));
-    grid->g.values = grid->values;
-    grid->g.band = band;
-    return WX_OK;
+    return wx::guard("wx_grid_set_values", [&]() -> int {
+        if (!ctx || !grid || !values) return fail(ctx, WX_ERR_INVALID, "wx_grid_set_values: null argument");
+        if (!(band > 0.0f) || !(band < 3.0e38f))
+            return fail(ctx, WX_ERR_INVALID, "wx_grid_set_values: band must be positive and finite");
+        WX_CUDA(ctx, cudaSetDevice(grid->device));
+        const size_t bytes = (size_t)grid->info.n3 * wx::kN3Slots * sizeof(float);
+        if (!grid->values && bytes) WX_CUDA(ctx, wx::dev_alloc(&grid->values, bytes));
+        if (bytes) WX_CUDA(ctx, cudaMemcpy(grid->values, values, bytes, cudaMemcpyHostToDevice));
+        grid->g.values = grid->values;
+        grid->g.band = band;
+        return WX_OK;
+    });
 }
 
 int wx_grid_get_info(const wx_grid *grid, wx_grid_info *out) {
-    if (!grid || !out) return WX_ERR_INVALID;
-    *out = grid->info;
-    return WX_OK;
+    return wx::guard("wx_grid_get_info", [&]() -> int {
+        if (!grid || !out) return WX_ERR_INVALID;
+        *out = grid->info;
+        return WX_OK;
+    });
 }
 
 int wx_render(wx_ctx *ctx, const wx_grid *grid, const wx_state_uniform *state, uint32_t width, uint32_t height,
               uint8_t *rgba8, wx_hit *hits, void *stream) {
-    if (!ctx || !grid || !state || !rgba8) return fail(ctx, WX_ERR_INVALID, "wx_render: null argument");
-    if (grid->device != ctx->device) return fail(ctx, WX_ERR_INVALID, "wx_render: grid is on another device");
-    if (((uintptr_t)rgba8 & 3) || ((uintptr_t)hits & 15))
-        return fail(ctx, WX_ERR_INVALID, "wx_render: rgba8 must be 4-byte and hits 16-byte aligned");
-    WX_CUDA(ctx, cudaSetDevice(ctx->device));
-    const uint32_t tiles_x = width / 8, tiles_y = height / 4;
-    const uint64_t ntiles = (uint64_t)tiles_x * tiles_y;
-    if (ntiles == 0) return WX_OK;
-    if ((uint64_t)width * height >= (1ull << 32)) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_render: frame too large");
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // Device memory and page-locked host memory are written by the kernel itself
-    // (page-locked memory through its device alias, over the host link while the
-    // march runs); pageable host memory goes through the context's staging buffer.
-    uint32_t *out_rgba = reinterpret_cast<uint32_t *>(rgba8);
-    wx_hit *out_hits = hits;
-    bool dev_rgba = device_accessible(rgba8);
-    bool dev_hits = hits ? device_accessible(hits) : true;
-    if (!dev_rgba) {
-        if (void *d = pinned_device_alias(rgba8)) {
-            out_rgba = static_cast<uint32_t *>(d);
-            dev_rgba = true;
-        }
-    }
-    if (!dev_hits) {
-        if (void *d = pinned_device_alias(hits)) {
-            out_hits = static_cast<wx_hit *>(d);
-            dev_hits = true;
-        }
-    }
-    const size_t npix = (size_t)width * height;
-    if (!dev_rgba || !dev_hits) {
-        const size_t need = npix * 4 + (hits ? npix * sizeof(wx_hit) + 256 : 0);
-        if (need > ctx->stage_bytes) {
-            if (ctx->stage) {
-                WX_CUDA(ctx, cudaStreamSynchronize(st));
-                cudaFree(ctx->stage);
+    return wx::guard("wx_render", [&]() -> int {
+        if (!ctx || !grid || !state || !rgba8) return fail(ctx, WX_ERR_INVALID, "wx_render: null argument");
+        if (grid->device != ctx->device) return fail(ctx, WX_ERR_INVALID, "wx_render: grid is on another device");
+        if (((uintptr_t)rgba8 & 3) || ((uintptr_t)hits & 15))
+            return fail(ctx, WX_ERR_INVALID, "wx_render: rgba8 must be 4-byte and hits 16-byte aligned");
+        WX_CUDA(ctx, cudaSetDevice(ctx->device));
+        const uint32_t tiles_x = width / 8, tiles_y = height / 4;
+        const uint64_t ntiles = (uint64_t)tiles_x * tiles_y;
+        if (ntiles == 0) return WX_OK;
+        if ((uint64_t)width * height >= (1ull << 32)) return fail(ctx, WX_ERR_UNSUPPORTED, "wx_render: frame too large");
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        // Device memory and page-locked host memory are written by the kernel itself
+        // (page-locked memory through its device alias, over the host link while the
+        // march runs); pageable host memory goes through the context's staging buffer.
+        uint32_t *out_rgba = reinterpret_cast<uint32_t *>(rgba8);
+        wx_hit *out_hits = hits;
+        bool dev_rgba = device_accessible(rgba8);
+        bool dev_hits = hits ? device_accessible(hits) : true;
+        if (!dev_rgba) {
+            if (void *d = pinned_device_alias(rgba8)) {
+                out_rgba = static_cast<uint32_t *>(d);
+                dev_rgba = true;
             }
-            ctx->stage = nullptr;
-            ctx->stage_bytes = 0;
-            WX_CUDA(ctx, wx::dev_alloc(&ctx->stage, need));
-            ctx->stage_bytes = need;
         }
-        char *b = static_cast<char *>(ctx->stage);
-        if (!dev_rgba) out_rgba = reinterpret_cast<uint32_t *>(b);
-        if (hits && !dev_hits) out_hits = reinterpret_cast<wx_hit *>(b + ((npix * 4 + 255) & ~(size_t)255));
-    }
-    const wxk::Job job = make_job(grid, *state, width, height, out_rgba, out_hits, 0, ctx->tuning);
-    if (ctx->tuning.kernel == 1) {
-        PixelOutputs cur{ctx->device, st, {0, 0}, {0, 0}};
-        cur.lo[0] = reinterpret_cast<uintptr_t>(out_rgba);
-        cur.hi[0] = cur.lo[0] + npix * 4;
-        if (hits) {
-            cur.lo[1] = reinterpret_cast<uintptr_t>(out_hits);
-            cur.hi[1] = cur.lo[1] + npix * sizeof(wx_hit);
+        if (!dev_hits) {
+            if (void *d = pinned_device_alias(hits)) {
+                out_hits = static_cast<wx_hit *>(d);
+                dev_hits = true;
+            }
         }
-        const cudaError_t e = launch_pixel_tracked(job, ctx->tuning, cur);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "wxk::launch_pixel");
-    } else {
-        WX_CUDA(ctx, wxk::launch_persistent(job, ctx->take_counter(), ctx->tuning, ctx->num_sms, st));
-    }
-    // Copy back only the dispatched region; the rest of a host buffer is untouched.
-    if (!dev_rgba)
-        WX_CUDA(ctx, cudaMemcpy2DAsync(rgba8, (size_t)width * 4, out_rgba, (size_t)width * 4, (size_t)tiles_x * 32,
-                                       (size_t)tiles_y * 4, cudaMemcpyDeviceToHost, st));
-    if (hits && !dev_hits)
-        WX_CUDA(ctx, cudaMemcpy2DAsync(hits, (size_t)width * sizeof(wx_hit), out_hits, (size_t)width * sizeof(wx_hit),
-                                       (size_t)tiles_x * 8 * sizeof(wx_hit), (size_t)tiles_y * 4,
-                                       cudaMemcpyDeviceToHost, st));
-    return WX_OK;
+        const size_t npix = (size_t)width * height;
+        if (!dev_rgba || !dev_hits) {
+            const size_t need = npix * 4 + (hits ? npix * sizeof(wx_hit) + 256 : 0);
+            if (need > ctx->stage_bytes) {
+                if (ctx->stage) {
+                    WX_CUDA(ctx, cudaStreamSynchronize(st));
+                    cudaFree(ctx->stage);
+                }
+                ctx->stage = nullptr;
+                ctx->stage_bytes = 0;
+                WX_CUDA(ctx, wx::dev_alloc(&ctx->stage, need));
+                ctx->stage_bytes = need;
+            }
+            char *b = static_cast<char *>(ctx->stage);
+            if (!dev_rgba) out_rgba = reinterpret_cast<uint32_t *>(b);
+            if (hits && !dev_hits) out_hits = reinterpret_cast<wx_hit *>(b + ((npix * 4 + 255) & ~(size_t)255));
+        }
+        const wxk::Job job = make_job(grid, *state, width, height, out_rgba, out_hits, 0, ctx->tuning);
+        if (ctx->tuning.kernel == 1) {
+            PixelOutputs cur{ctx->device, st, {0, 0}, {0, 0}};
+            cur.lo[0] = reinterpret_cast<uintptr_t>(out_rgba);
+            cur.hi[0] = cur.lo[0] + npix * 4;
+            if (hits) {
+                cur.lo[1] = reinterpret_cast<uintptr_t>(out_hits);
+                cur.hi[1] = cur.lo[1] + npix * sizeof(wx_hit);
+            }
+            const cudaError_t e = launch_pixel_tracked(job, ctx->tuning, cur);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "wxk::launch_pixel");
+        } else {
+            WX_CUDA(ctx, wxk::launch_persistent(job, ctx->take_counter(), ctx->tuning, ctx->num_sms, st));
+        }
+        // Copy back only the dispatched region; the rest of a host buffer is untouched.
+        if (!dev_rgba)
+            WX_CUDA(ctx, cudaMemcpy2DAsync(rgba8, (size_t)width * 4, out_rgba, (size_t)width * 4, (size_t)tiles_x * 32,
+                                           (size_t)tiles_y * 4, cudaMemcpyDeviceToHost, st));
+        if (hits && !dev_hits)
+            WX_CUDA(ctx, cudaMemcpy2DAsync(hits, (size_t)width * sizeof(wx_hit), out_hits, (size_t)width * sizeof(wx_hit),
+                                           (size_t)tiles_x * 8 * sizeof(wx_hit), (size_t)tiles_y * 4,
+                                           cudaMemcpyDeviceToHost, st));
+        return WX_OK;
+    });
 }
 
 // ---- batched rendering: many frames of several grids in one persistent launch ----
@@ -1110,29 +1142,35 @@ int wx_batch_create(wx_ctx *ctx, const wx_frame *frames, uint32_t n, wx_batch **
 }
 
 int wx_batch_launch(wx_batch *b, void *stream) {
-    if (!b) return WX_ERR_INVALID;
-    WX_CUDA(b->ctx, cudaSetDevice(b->ctx->device));
-    WX_CUDA(b->ctx, cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream)));
-    return WX_OK;
+    return wx::guard("wx_batch_launch", [&]() -> int {
+        if (!b) return WX_ERR_INVALID;
+        WX_CUDA(b->ctx, cudaSetDevice(b->ctx->device));
+        WX_CUDA(b->ctx, cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream)));
+        return WX_OK;
+    });
 }
 
 int wx_batch_info(const wx_batch *b, uint32_t *frames, uint32_t *tiles, uint64_t *rays) {
-    if (!b) return WX_ERR_INVALID;
-    if (frames) *frames = b->njobs;
-    if (tiles) *tiles = b->total_tiles;
-    if (rays) *rays = b->rays;
-    return WX_OK;
+    return wx::guard("wx_batch_info", [&]() -> int {
+        if (!b) return WX_ERR_INVALID;
+        if (frames) *frames = b->njobs;
+        if (tiles) *tiles = b->total_tiles;
+        if (rays) *rays = b->rays;
+        return WX_OK;
+    });
 }
 
 int wx_batch_destroy(wx_batch *b) {
-    if (!b) return WX_OK;
-    cudaSetDevice(b->ctx->device);
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->graph) cudaGraphDestroy(b->graph);
-    if (b->jobs_dev) cudaFree(b->jobs_dev);
-    if (b->counter) cudaFree(b->counter);
-    delete b;
-    return WX_OK;
+    return wx::guard("wx_batch_destroy", [&]() -> int {
+        if (!b) return WX_OK;
+        cudaSetDevice(b->ctx->device);
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        if (b->jobs_dev) cudaFree(b->jobs_dev);
+        if (b->counter) cudaFree(b->counter);
+        delete b;
+        return WX_OK;
+    });
 }
 
 }  // extern "C"
