@@ -27,7 +27,7 @@ def test_parity_suites_in_the_bounds_checked_build():
         pytest.skip("already the bounds-checked build")
     env = dict(os.environ, WOXEL_GB300_BOUNDS_CHECK="1")
     suites = ["tests/test_render_gpu.py", "tests/test_fuzz_gpu.py", "tests/test_batch_gpu.py",
-              "tests/test_surface_gpu.py", "tests/test_chain_gpu.py"]
+              "tests/test_surface_gpu.py", "tests/test_chain_gpu.py", "tests/test_wgsl_golden_gpu.py"]
     r = subprocess.run([sys.executable, "-m", "pytest", *suites, "-m", "gpu", "-q", "-x", "-p", "no:cacheprovider"],
                        cwd=ROOT, env=env, capture_output=True, text=True, timeout=1800)
     assert r.returncode == 0, r.stdout[-4000:] + r.stderr[-2000:]

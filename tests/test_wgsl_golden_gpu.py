@@ -4,8 +4,10 @@ The frames of tests/golden/wgsl_raycast.npz come from src/shaders/raycast.comp.w
 (woxel) translated mechanically to C++ and run on the host (see test_wgsl_golden.py).
 Here the product renders the same uniforms over the same grids, handed to it as the
 reference's flattened view (masks, origins, atlases built by the oracle) through the
-drop-in upload, with and without hit records, through both kernel families; every
-RGBA8 byte must be equal. This includes the benchmark's first 1920x1080 frame of the
+drop-in upload, with and without hit records, through every kernel (one pixel per
+lane, persistent warps, lanes that refill, one batched launch and its CUDA-graph plan);
+every RGBA8 byte must be equal. The bounds-checked build reruns this file
+(tests/test_bounds_gpu.py). This includes the benchmark's first 1920x1080 frame of the
 2000-sphere grid, which the fixture holds whole.
 """
 import numpy as np
@@ -42,10 +44,11 @@ def _check(golden, ctx, grids, hits):
     assert n == len(golden["meta"])
 
 
-@pytest.mark.parametrize("kernel", [1, 0])
-def test_kernels_match_reference_shader(golden, cuda_ctx, grids, kernel):
+@pytest.mark.parametrize("kernel,rays", [(1, 1), (0, 1), (1, 2), (1, 4)])
+def test_kernels_match_reference_shader(golden, cuda_ctx, grids, kernel, rays):
+    """k_pixel, the persistent kernel, and k_wave's lane refill (2 and 4 rays per lane)."""
     old = cuda_ctx.tuning
-    cuda_ctx.set_tuning(kernel=kernel)
+    cuda_ctx.set_tuning(kernel=kernel, rays_per_lane=rays)
     try:
         _check(golden, cuda_ctx, grids, hits=False)
     finally:
