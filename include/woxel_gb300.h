@@ -264,8 +264,8 @@ int wx_batch_destroy(wx_batch *batch);
  * device (else WX_ERR_INVALID); outputs in device memory; default launch shape
  * (8x4 tiles).
  * The first call on a device does a one-time set-up on that device (it looks
- * up the array's device address and loads the kernels' division table): make
- * that first call before any stream capture. The frame table reaches the array
+ * up the array's device address and loads the kernels' division table). The
+ * frame table reaches the array
  * through the parameters of small table-writing kernels, which the runtime
  * copies when they are enqueued, so the call does not wait for the GPU and a
  * later call cannot change the table of an earlier one. Every call reuses the
